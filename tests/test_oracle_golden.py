@@ -1,0 +1,49 @@
+"""Checks the FP64 oracle against fixtures made by the reference's own
+sources (tests/golden/make_golden.py); runs on any machine."""
+import numpy as np
+
+from oracle import oracle as O
+from autoscoper_gb300 import scene as S
+from golden_scene import load
+
+
+def test_volume_constants():
+    sc, z = load()
+    vd = O.VolumeDesc(sc.volumes[0])
+    assert np.array_equal(vd.inv_scale, z["inv_scale"]) and np.array_equal(vd.inv_trans, z["inv_trans"])
+    assert np.array_equal(vd.trans_center, z["trans_center"])
+    assert np.float32(vd.min_value) == z["minmax"][0] and np.float32(vd.max_value) == z["minmax"][1]
+
+
+def test_views_against_reference_outputs():
+    sc, z = load()
+    tr = O.Tracker(sc)
+    for vi in range(2):
+        v = sc.views[vi]
+        rp = sc.ray[vi][0]
+        for k, pose in enumerate(z["poses"]):
+            key = f"v{vi}p{k}"
+            xc = O.frame_from_xyzypr(pose)
+            mv = O.frame_mul(O.frame_inverse(v.camera.frame), xc)
+            assert np.array_equal(O.frame_row_matrix(O.frame_inverse(mv)), z[key + "_imv"])
+            ok, m, vp, w, h = tr.view_setup(0, vi, pose)
+            assert ok and np.array_equal(vp, z[key + "_vp"])
+            drr = O.raycast(tr.vd[0], m, np.float32(vp).astype(np.float64), float(np.float32(rp.step)),
+                            float(np.float32(rp.intensity)), float(np.float32(rp.cutoff)), w, h)
+            d = np.abs(drr - z[key + "_drr"])
+            assert np.mean(d > 1e-5) < 2e-3 and d.max() < 2.5 * rp.step * rp.cutoff / rp.intensity + 1e-5
+            rad = O.image_render(v.radiograph, np.float32(v.camera.viewport).astype(np.float64),
+                                 np.float32(vp).astype(np.float64), w, h)
+            assert np.abs(rad - z[key + "_rad"]).max() < 2e-5
+            # NCC / SAD of the reference's own masked images through the oracle
+            ncc = 1.0 - tr.track_frame(0, pose)[vi]
+            assert abs(ncc - float(z[key + "_ncc"])) < 5e-4
+
+
+def test_filters_against_reference_outputs():
+    _, z = load()
+    x = z["filter_in"]
+    assert np.abs(O.apply_filter(S.Filter.sobel(0.43, 3.0), x) - z["sobel"]).max() < 3e-6
+    assert np.abs(O.apply_filter(S.Filter.contrast_filter(2.5, 0.9), x) - z["contrast"]).max() < 2e-5
+    assert np.abs(O.apply_filter(S.Filter.gaussian(1.5), x) - z["gaussian"]).max() < 3e-6
+    assert np.mean(np.abs(O.apply_filter(S.Filter.sharpen(1.0, 2.0, 0.01), x) - z["sharpen"]) > 1e-5) < 2e-3
