@@ -1,0 +1,308 @@
+"""Python face of the C ABI: device buffers, volumes, images, the plain
+operators and the batched engine.  Thin wrappers only; all work runs in
+libautoscoper_gb300.so on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from . import scene as S
+
+
+def lib():
+    return L.load()
+
+
+class DeviceArray:
+    """A cudaMalloc'd buffer holding a numpy-shaped array."""
+
+    def __init__(self, shape, dtype=np.float32):
+        self.shape = tuple(shape) if not isinstance(shape, int) else (shape,)
+        self.dtype = np.dtype(dtype)
+        self.nbytes = int(np.prod(self.shape)) * self.dtype.itemsize
+        p = C.c_void_p()
+        L.call("asc_malloc", C.byref(p), max(self.nbytes, 1))
+        self.ptr = p.value
+
+    @classmethod
+    def from_host(cls, a, stream=None):
+        a = np.ascontiguousarray(a)
+        d = cls(a.shape, a.dtype)
+        if a.nbytes:
+            L.call("asc_memcpy_h2d", d.ptr, a.ctypes.data, a.nbytes, stream)
+            L.call("asc_stream_sync", stream)
+        return d
+
+    def to_host(self, stream=None):
+        a = np.empty(self.shape, self.dtype)
+        if a.nbytes:
+            L.call("asc_memcpy_d2h", a.ctypes.data, self.ptr, a.nbytes, stream)
+        return a
+
+    def upload(self, a, stream=None):
+        a = np.ascontiguousarray(a, dtype=self.dtype)
+        assert a.nbytes <= self.nbytes
+        L.call("asc_memcpy_h2d", self.ptr, a.ctypes.data, a.nbytes, stream)
+
+    def free(self):
+        if getattr(self, "ptr", None):
+            lib().asc_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _d(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _f(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a, a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class DeviceVolume:
+    """VolumeDescription on the device (asc_volume_create)."""
+
+    def __init__(self, vol: S.Volume, storage=L.ASC_STORE_U16):
+        data = np.ascontiguousarray(vol.data)
+        D, H, W = data.shape
+        sc, scp = _d(vol.scale)
+        fl = (C.c_int * 3)(*[int(x) for x in vol.flip])
+        h = C.c_void_p()
+        L.call("asc_volume_create", data.ctypes.data, W, H, D, 8 * data.dtype.itemsize, scp, fl, storage, C.byref(h))
+        self.handle = h.value
+        self.storage = storage
+        isc = (C.c_float * 3)()
+        itr = (C.c_float * 3)()
+        tc = (C.c_double * 3)()
+        mn, mx = C.c_float(), C.c_float()
+        dims = (C.c_int * 3)()
+        L.call("asc_volume_info", self.handle, isc, itr, tc, C.byref(mn), C.byref(mx), dims)
+        self.inv_scale = np.array(isc[:], np.float32)
+        self.inv_trans = np.array(itr[:], np.float32)
+        self.trans_center = np.array(tc[:])
+        self.min_value, self.max_value = mn.value, mx.value
+        self.dims = tuple(dims[:])
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().asc_volume_destroy(self.handle)
+        except Exception:
+            pass
+
+
+class DeviceImage:
+    """A radiograph (u8/u16) or background (float32) on the device."""
+
+    def __init__(self, img):
+        img = np.ascontiguousarray(img)
+        bps = 32 if img.dtype == np.float32 else 8 * img.dtype.itemsize
+        h = C.c_void_p()
+        L.call("asc_image_create", img.ctypes.data, img.shape[1], img.shape[0], bps, C.byref(h))
+        self.handle = h.value
+        self.shape = img.shape
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().asc_image_destroy(self.handle)
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- plain operators (host arrays in/out)
+
+def raycast(vol: DeviceVolume, imv16, viewport, step, intensity, cutoff, w, h, visible=True, out=None):
+    o = out or DeviceArray((h, w))
+    _, mp = _d(imv16)
+    _, vpp = _f(viewport)
+    L.call("asc_raycast", vol.handle, mp, vpp, step, intensity, cutoff, int(visible), o.ptr, w, h, None)
+    return o
+
+
+def rad_render(img: DeviceImage, image_plane, viewport, w, h, out=None):
+    o = out or DeviceArray((h, w))
+    _, ipp = _f(image_plane)
+    _, vpp = _f(viewport)
+    L.call("asc_rad_render", img.handle, ipp, vpp, o.ptr, w, h, None)
+    return o
+
+
+def background_render(img: DeviceImage, image_plane, viewport, threshold, w, h, out=None):
+    o = out or DeviceArray((h, w))
+    _, ipp = _f(image_plane)
+    _, vpp = _f(viewport)
+    L.call("asc_background_render", img.handle, ipp, vpp, threshold, o.ptr, w, h, None)
+    return o
+
+
+def apply_filter(flt: S.Filter, src: DeviceArray, out=None):
+    h, w = src.shape
+    o = out or DeviceArray((h, w))
+    if flt.kind == S.SOBEL:
+        L.call("asc_sobel", src.ptr, o.ptr, w, h, flt.scale, flt.blend, None)
+    elif flt.kind == S.CONTRAST:
+        L.call("asc_contrast", src.ptr, o.ptr, w, h, flt.alpha, flt.beta, flt.size, None)
+    elif flt.kind == S.GAUSSIAN:
+        L.call("asc_gaussian", src.ptr, o.ptr, w, h, flt.radius, None)
+    elif flt.kind == S.SHARPEN:
+        L.call("asc_sharpen", src.ptr, o.ptr, w, h, flt.radius, flt.contrast, flt.threshold, None)
+    else:
+        raise ValueError(flt.kind)
+    return o
+
+
+def ncc(f: DeviceArray, g: DeviceArray, mask: DeviceArray, coverage=L.ASC_SUM_TREE) -> float:
+    r = C.c_double()
+    L.call("asc_ncc_host", f.ptr, g.ptr, mask.ptr, int(np.prod(f.shape)), coverage, C.byref(r), None)
+    return r.value
+
+
+def hdist(f: DeviceArray, g: DeviceArray, mask: DeviceArray, coverage=L.ASC_SUM_TREE) -> float:
+    r = C.c_double()
+    L.call("asc_hdist_host", f.ptr, g.ptr, mask.ptr, int(np.prod(f.shape)), coverage, C.byref(r), None)
+    return r.value
+
+
+def elementwise(name, *srcs, out=None):
+    h, w = srcs[0].shape
+    o = out or DeviceArray((h, w) if name != "asc_composite" else (h, w, 3))
+    args = [s.ptr for s in srcs]
+    if name == "asc_composite":
+        args.append(srcs[2].ptr)
+    L.call(name, *args, o.ptr, w, h, None)
+    return o
+
+
+# ---------------------------------------------------------------- engine
+
+def _filters(lst, arr):
+    n = 0
+    for f in lst:
+        if f.kind == S.SOBEL:
+            p = (f.scale, f.blend, 0.0)
+        elif f.kind == S.CONTRAST:
+            p = (f.alpha, f.beta, float(f.size))
+        elif f.kind == S.GAUSSIAN:
+            p = (f.radius, 0.0, 0.0)
+        elif f.kind == S.SHARPEN:
+            p = (f.radius, f.contrast, f.threshold)
+        else:
+            raise ValueError(f.kind)
+        arr[n] = L.FilterDesc(f.kind, int(f.enabled), *p)
+        n += 1
+    return n
+
+
+class Engine:
+    """A scene resident on the device (asc_engine_create) that scores
+    (bone, manipulator) candidates with Tracker::minimizationFunc semantics."""
+
+    def __init__(self, scene: S.Scene, max_items=256, coverage=L.ASC_SUM_TREE, storage=L.ASC_STORE_U16,
+                 volumes=None, images=None):
+        self.scene = scene
+        self.vols = volumes or [DeviceVolume(v, storage) for v in scene.volumes]
+        self.rads = images or [DeviceImage(v.radiograph) for v in scene.views]
+        self.bgs = [DeviceImage(v.background) if v.background is not None else None for v in scene.views]
+        nv, nb = len(scene.views), len(scene.volumes)
+        views = (L.ViewDesc * nv)()
+        for i, v in enumerate(scene.views):
+            d = views[i]
+            d.frame[:] = list(v.camera.frame)
+            d.viewport[:] = list(v.camera.viewport)
+            d.image_plane[:] = list(v.camera.image_plane)
+            d.radiograph = self.rads[i].handle
+            d.background = self.bgs[i].handle if self.bgs[i] else None
+            d.bg_threshold = v.bg_threshold
+            d.n_drr_filters = _filters(v.drr_filters, d.drr_filters)
+            d.n_rad_filters = _filters(v.rad_filters, d.rad_filters)
+        bones = (L.BoneDesc * nb)()
+        for b in range(nb):
+            d = bones[b]
+            d.volume = self.vols[b].handle
+            d.pivot[:] = list(scene.pivots[b])
+            d.base_pose[:] = [float(x) for x in np.asarray(scene.poses[b], np.float32)]
+            for v in range(nv):
+                rp = scene.ray[v][b]
+                d.step[v], d.intensity[v], d.cutoff[v] = rp.step, rp.intensity, rp.cutoff
+        h = C.c_void_p()
+        L.call("asc_engine_create", nv, views, nb, bones, scene.render_width, scene.render_height, max_items,
+               coverage, scene.cf_model, C.byref(h))
+        self.handle = h.value
+        self.n_views = nv
+        self.max_items = max_items
+
+    def set_base_pose(self, bone, xyzypr):
+        _, p = _d(np.asarray(xyzypr, np.float32).astype(np.float64))
+        L.call("asc_engine_set_base_pose", self.handle, bone, p)
+
+    def set_radiograph(self, view, img: DeviceImage):
+        L.call("asc_engine_set_radiograph", self.handle, view, img.handle)
+        self.rads[view] = img
+
+    def eval(self, bones, manips, plain=False):
+        """Costs (n,) and per-view costs (n, n_views) of candidates."""
+        b = np.ascontiguousarray(bones, dtype=np.int32)
+        m = np.ascontiguousarray(manips, dtype=np.float64).reshape(-1, 6)
+        n = len(b)
+        cost = np.zeros(n)
+        vcost = np.zeros((n, self.n_views))
+        fn = "asc_engine_eval_plain" if plain else "asc_engine_eval_host"
+        L.call(fn, self.handle, n, b.ctypes.data_as(C.POINTER(C.c_int)), m.ctypes.data_as(C.POINTER(C.c_double)),
+               cost.ctypes.data_as(C.POINTER(C.c_double)), vcost.ctypes.data_as(C.POINTER(C.c_double)), None)
+        return cost, vcost
+
+    def eval_device(self, n, bone_dev: DeviceArray, manip_dev: DeviceArray, cost_dev: DeviceArray, stream=None):
+        L.call("asc_engine_eval", self.handle, n, bone_dev.ptr, manip_dev.ptr, cost_dev.ptr, None, stream)
+
+    def pso(self, n_particles=100, n_iter=50, w=0.7298, c1=1.4962, c2=1.4962, lo=-6.0, hi=6.0, seed=1):
+        nb = len(self.scene.volumes)
+        best = np.zeros((nb, 6))
+        cost = np.zeros(nb)
+        ev = C.c_longlong()
+        L.call("asc_engine_pso", self.handle, n_particles, n_iter, w, c1, c2, lo, hi, seed,
+               best.ctypes.data_as(C.POINTER(C.c_double)), cost.ctypes.data_as(C.POINTER(C.c_double)),
+               C.byref(ev), None)
+        return best, cost, ev.value
+
+    def debug_layout(self, n):
+        d, lay = C.c_void_p(), C.c_void_p()
+        L.call("asc_engine_debug", self.handle, C.byref(d), C.byref(lay))
+        return d.value, lay.value
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().asc_engine_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def pso_sequential(cost, n_particles=100, lo=-1.0, hi=1.0, epochs=50, stall=25, seed=0):
+    """Reference-sequential PSO on the host (asc_pso_sequential)."""
+    cb = L.COST_FN(lambda p, ctx: float(cost([p[i] for i in range(6)])))
+    pos = (C.c_float * 6)()
+    val = C.c_float()
+    L.call("asc_pso_sequential", cb, None, n_particles, lo, hi, epochs, stall, seed, pos, C.byref(val))
+    return np.array(pos[:], np.float32), float(val.value)
+
+
+def amoeba(cost, P, Y, ftol=1e-3):
+    P = np.ascontiguousarray(P, dtype=np.float64).copy()
+    Y = np.ascontiguousarray(Y, dtype=np.float64).copy()
+    ndim = P.shape[1]
+    cb = L.COST_FN(lambda p, ctx: float(cost(np.array([p[i] for i in range(ndim)]))))
+    it = C.c_int()
+    L.call("asc_amoeba", cb, None, P.ctypes.data_as(C.POINTER(C.c_double)),
+           Y.ctypes.data_as(C.POINTER(C.c_double)), ndim, ftol, C.byref(it))
+    return P, Y, it.value

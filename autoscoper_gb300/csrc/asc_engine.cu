@@ -1,0 +1,1131 @@
+// Batched registration engine: Tracker::minimizationFunc (Tracker.cpp:775-827)
+// for many (bone, manipulator) candidates per pass, with the scene resident
+// on the device.
+//
+// One evaluation is four launches on one stream:
+//   k_setup       1 block:  FP64 pose composition, view matrices, viewports
+//                            (Tracker.cpp:603-634) and the tile layout of every
+//                            (item, view) crop, with prefix sums;
+//   k_ray         persistent: 16x16-ray tiles pulled from an atomic queue,
+//                            DRRs written to a packed buffer;
+//   k_view        persistent: 32x32 output tiles pulled from a queue; each
+//                            stages DRR and radiograph regions with the chain's
+//                            halo in shared memory, runs both filter chains,
+//                            the masks and the NCC moments; the last tile of a
+//                            view merges its tiles in FP64, the last view of an
+//                            item sums the view costs.
+// The PSO driver adds an update kernel before and a best-update kernel after,
+// and captures one iteration as a CUDA graph.
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "asc_internal.cuh"
+
+namespace asc {
+const void* image_data(asc_image im, int* w, int* h, int* bps);
+}
+
+using namespace asc;
+
+namespace {
+
+constexpr int MAX_VIEWS = 4;
+constexpr int MAX_BONES = 16;
+constexpr int MAX_FILTERS = 8;
+constexpr int VT = 32;   // k_view output tile edge
+constexpr int RT = 16;   // k_ray tile edge
+
+struct FilterDev {
+  int kind, K, R;
+  float p0, p1, p2;
+  float g[32];
+};
+
+struct ViewDev {
+  double cam[12], cam_inv[12], ip[12], cvp[4];
+  float ipf[4];
+  const void* rad;
+  int rad_w, rad_h, rad_bps;
+  const float* bg;
+  int bg_w, bg_h;
+  float bg_thr;
+  int n_drr, n_rad, h_drr, h_rad;
+  FilterDev fdrr[MAX_FILTERS], frad[MAX_FILTERS];
+};
+
+struct BoneDev {
+  DevVolume vol;
+  float inv_scale[3], inv_trans[3];
+  double pivot[12], pivot_inv[12], base[6];
+  float step[MAX_VIEWS], scale[MAX_VIEWS], cutoff_raw[MAX_VIEWS];
+};
+
+struct SceneDev {
+  int n_views, n_bones, rw, rh, coverage, E;
+  ViewDev views[MAX_VIEWS];
+  BoneDev bones[MAX_BONES];
+};
+
+struct IV {
+  float m[12];
+  float vp[4];
+  int w, h, ok, bone;
+  int rtx, rty, ftx, fty;
+  long long pix;  // offset of this crop in the DRR buffer
+};
+
+struct Counters {
+  int n_items, n_iv;
+  int rtiles, ftiles;
+  int rnext, fnext;
+  int error;
+  int pad;
+  unsigned long long samples, pixels;
+};
+
+struct Bufs {
+  IV* iv;
+  int* roff;       // n_iv + 1 prefix of ray tiles
+  int* foff;       // n_iv + 1 prefix of view tiles
+  float* drr;
+  Moments* part;   // per view tile
+  double* vcost;   // per iv
+  unsigned* ivt;   // per-iv tile tickets
+  unsigned* itt;   // per-item view tickets
+  Counters* C;
+};
+
+__device__ __forceinline__ int find_iv(const int* off, int n, int tile)
+{
+  int lo = 0, hi = n;  // off[lo] <= tile < off[hi]
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(off + mid) <= tile) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ void finish_item(const SceneDev* sc, const Bufs& b, int item, double* cost)
+{
+  double tot = 0;
+  for (int v = 0; v < sc->n_views; ++v) tot += b.vcost[item * sc->n_views + v];
+  cost[item] = tot < 0 ? 9999.0 : tot;  // Tracker.cpp:823-825
+}
+
+// ---------------------------------------------------------------- k_setup
+__global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc, int n_items,
+                                                 const int* __restrict__ bone_in, const double* __restrict__ manip,
+                                                 Bufs b, double* __restrict__ cost, double* __restrict__ view_cost_out)
+{
+  __shared__ int s_err;
+  const int nv = sc->n_views, n_iv = n_items * nv;
+  const int per = (n_iv + blockDim.x - 1) / blockDim.x;
+  const int i0 = threadIdx.x * per, i1 = min(i0 + per, n_iv);
+  if (threadIdx.x == 0) s_err = 0;
+  __syncthreads();
+  int rsum = 0, fsum = 0;
+  long long psum = 0;
+  for (int k = i0; k < i1; ++k) {
+    const int item = k / nv, v = k % nv;
+    IV r;
+    memset(&r, 0, sizeof r);
+    int bi = bone_in[item];
+    if (bi < 0 || bi >= sc->n_bones) bi = 0;
+    r.bone = bi;
+    const BoneDev& B = sc->bones[bi];
+    const ViewDev& V = sc->views[v];
+    // minimizationFunc: pose . V^-1 . manip . V, then the xyzypr round trip
+    double base[12], man[12], t1[12], t2[12], xyz[6];
+    frame_from_xyzypr(B.base, base);
+    frame_from_axis_angle(manip + 6 * item, man);
+    frame_mul(base, B.pivot_inv, t1);
+    frame_mul(t1, man, t2);
+    frame_mul(t2, B.pivot, t1);
+    frame_to_xyzypr(t1, xyz);
+    frame_from_xyzypr(xyz, t1);
+    // trackFrame (1a)-(1c)
+    double mv[12], imv[12], imv16[16], vp[4];
+    frame_mul(V.cam_inv, t1, mv);
+    frame_inverse(mv, imv);
+    frame_row_matrix(imv, imv16);
+    fold_matrix(imv16, B.inv_scale, B.inv_trans, r.m);
+    double vc = 0.0;
+    if (!calculate_viewport(mv, V.cam, V.ip, B.inv_scale, B.inv_trans, vp)) {
+      vc = 9999.0;  // Tracker.cpp:614-617
+    } else {
+      double fw = vp[2] * sc->rw / V.cvp[2], fh = vp[3] * sc->rh / V.cvp[3];
+      unsigned w = fw > 0 ? (unsigned)fw : 0u, h = fh > 0 ? (unsigned)fh : 0u;
+      if (w > (unsigned)sc->rw || h > (unsigned)sc->rh) {
+        s_err = ASC_ERR_RANGE;  // the reference throws (Tracker.cpp:625-629)
+        w = 0;
+        h = 0;
+      }
+      r.w = (int)w;
+      r.h = (int)h;
+      for (int j = 0; j < 4; ++j) r.vp[j] = (float)vp[j];
+      if (w == 0 || h == 0) {
+        vc = 1.0 - 1e5;  // degenerate NCC of an empty crop
+      } else {
+        r.ok = 1;
+        r.rtx = (r.w + RT - 1) / RT;
+        r.rty = (r.h + RT - 1) / RT;
+        r.ftx = (r.w + VT - 1) / VT;
+        r.fty = (r.h + VT - 1) / VT;
+      }
+    }
+    r.pix = psum;  // local offset, fixed up after the scan
+    psum += (long long)r.w * r.h;
+    rsum += r.rtx * r.rty;
+    fsum += r.ftx * r.fty;
+    b.iv[k] = r;
+    b.vcost[k] = vc;
+    b.ivt[k] = 0;
+  }
+  // block-wide exclusive scan of (rsum, fsum, psum)
+  __shared__ long long sp[1024];
+  __shared__ int sr[1024], sf[1024];
+  sr[threadIdx.x] = rsum;
+  sf[threadIdx.x] = fsum;
+  sp[threadIdx.x] = psum;
+  __syncthreads();
+  for (int o = 1; o < blockDim.x; o <<= 1) {
+    int a = threadIdx.x >= o ? sr[threadIdx.x - o] : 0;
+    int c = threadIdx.x >= o ? sf[threadIdx.x - o] : 0;
+    long long p = threadIdx.x >= o ? sp[threadIdx.x - o] : 0;
+    __syncthreads();
+    sr[threadIdx.x] += a;
+    sf[threadIdx.x] += c;
+    sp[threadIdx.x] += p;
+    __syncthreads();
+  }
+  int rbase = sr[threadIdx.x] - rsum, fbase = sf[threadIdx.x] - fsum;
+  long long pbase = sp[threadIdx.x] - psum;
+  for (int k = i0; k < i1; ++k) {
+    IV& r = b.iv[k];
+    r.pix += pbase;
+    b.roff[k] = rbase;
+    b.foff[k] = fbase;
+    rbase += r.rtx * r.rty;
+    fbase += r.ftx * r.fty;
+  }
+  if (threadIdx.x == blockDim.x - 1) {
+    b.roff[n_iv] = rbase;
+    b.foff[n_iv] = fbase;
+    b.C->n_items = n_items;
+    b.C->n_iv = n_iv;
+    b.C->rtiles = rbase;
+    b.C->ftiles = fbase;
+    b.C->rnext = 0;
+    b.C->fnext = 0;
+    b.C->error = s_err;
+    b.C->samples = 0;
+    b.C->pixels = (unsigned long long)(sp[threadIdx.x]);
+  }
+  __syncthreads();
+  // item tickets: views finished here count as arrived
+  for (int item = threadIdx.x; item < n_items; item += blockDim.x) {
+    unsigned pre = 0;
+    for (int v = 0; v < nv; ++v) pre += b.iv[item * nv + v].ok ? 0u : 1u;
+    b.itt[item] = pre;
+    if (pre == (unsigned)nv) finish_item(sc, b, item, cost);
+  }
+  (void)view_cost_out;
+}
+
+// ---------------------------------------------------------------- k_ray
+template <int STORE>
+__device__ __forceinline__ float march_any(const DevVolume& V, const RaySetup& r, float cut)
+{
+  return march<STORE>(V, r.X0, r.dX, r.Y0, r.dY, r.Z0, r.dZ, r.tnear, r.tfar, cut);
+}
+
+__global__ void __launch_bounds__(256) k_ray(const SceneDev* __restrict__ sc, Bufs b)
+{
+  __shared__ int s_tile;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ox = (warp & 1) * 8 + (lane & 7), oy = (warp >> 1) * 4 + (lane >> 3);
+  const int nv = sc->n_views;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(&b.C->rnext, 1);
+    __syncthreads();
+    const int tile = s_tile;
+    __syncthreads();
+    if (tile >= b.C->rtiles) return;
+    const int k = find_iv(b.roff, b.C->n_iv, tile);
+    const IV& r = b.iv[k];
+    const int t = tile - b.roff[k];
+    const int x = (t % r.rtx) * RT + ox, y = (t / r.rtx) * RT + oy;
+    if (x >= r.w || y >= r.h) continue;
+    const BoneDev& B = sc->bones[r.bone];
+    const int v = k % nv;
+    RaySetup rs;
+    float d = 0.f;
+    const bool hit = ray_setup(r.m, r.vp, x, y, r.w, r.h, B.step[v], B.vol.nx, B.vol.ny, B.vol.nz, rs);
+    {
+      // trilinear samples of this ray (the work figure of the roofline)
+      unsigned cnt = hit ? (unsigned)ceilf(rs.tfar - rs.tnear) : 0u;
+      unsigned mask = __activemask();
+      unsigned tot = __reduce_add_sync(mask, cnt);
+      if ((int)(threadIdx.x & 31) == __ffs(mask) - 1) atomicAdd(&b.C->samples, (unsigned long long)tot);
+    }
+    if (hit) {
+      float cut = B.cutoff_raw[v];
+      float acc;
+      if (B.vol.storage == ASC_STORE_BF16)
+        acc = march_any<ASC_STORE_BF16>(B.vol, rs, cut);
+      else if (B.vol.storage == ASC_STORE_F16)
+        acc = march_any<ASC_STORE_F16>(B.vol, rs, cut);
+      else
+        acc = march_any<ASC_STORE_U16>(B.vol, rs, cut);
+      d = acc * B.scale[v];
+    }
+    b.drr[r.pix + (long long)y * r.w + x] = fminf(fmaxf(d, 0.f), 1.f);
+  }
+}
+
+// ---------------------------------------------------------------- k_view
+// Region coordinates: buffer index (ry, rx) <-> image (y0 + ry, x0 + rx) with
+// x0 = tile x - E_h, where E_h = (E - VT) / 2 is the largest chain halo.
+struct Region {
+  int x0, y0, E, w, h;
+};
+
+__device__ __forceinline__ bool inside(const Region& g, int ry, int rx)
+{
+  int x = g.x0 + rx, y = g.y0 + ry;
+  return x >= 0 && x < g.w && y >= 0 && y < g.h;
+}
+
+// Applies one filter from `in` to `out` over the square band
+// [lo, hi) x [lo, hi) of region coordinates; positions outside the image get
+// 0.  `tmp` holds the horizontal pass of a Gaussian/Sharpen blur.
+__device__ void apply_stage(const FilterDev& f, const float* in, float* out, float* tmp, const Region& g, int lo,
+                            int hi)
+{
+  const int E = g.E, n = hi - lo;
+  if (f.kind == 3 || f.kind == 4) {
+    const int R = f.R;
+    // horizontal pass over rows [lo - R, hi + R)
+    const int rows = n + 2 * R;
+    for (int i = threadIdx.x; i < rows * n; i += blockDim.x) {
+      int ry = lo - R + i / n, rx = lo + i % n;
+      const float* p = in + ry * E + rx - R;
+      float s = 0.f;
+      for (int k = 0; k < f.K; ++k) s = fmaf(f.g[k], p[k], s);
+      tmp[ry * E + rx] = s;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+      int ry = lo + i / n, rx = lo + i % n;
+      float r = 0.f;
+      if (inside(g, ry, rx)) {
+        float blur = 0.f;
+        for (int k = 0; k < f.K; ++k) blur = fmaf(f.g[k], tmp[(ry - R + k) * E + rx], blur);
+        if (f.kind == 3) {
+          r = fminf(fmaxf(blur, 0.f), 1.f);
+        } else {
+          float v = in[ry * E + rx];
+          r = fabsf(v - blur) > f.p2 ? fminf(fmaxf(v + f.p1 * (v - blur), 0.f), 1.f) : v;
+        }
+      }
+      out[ry * E + rx] = r;
+    }
+  } else if (f.kind == 1) {
+    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+      int ry = lo + i / n, rx = lo + i % n;
+      float r = 0.f;
+      if (inside(g, ry, rx)) {
+        int x = g.x0 + rx, y = g.y0 + ry;
+        int xm = x > 0 ? -1 : 0, xp = x < g.w - 1 ? 1 : 0, ym = y > 0 ? -1 : 0, yp = y < g.h - 1 ? 1 : 0;
+        const float* c = in + ry * E + rx;
+        float p00 = c[ym * E + xm], p01 = c[ym * E], p02 = c[ym * E + xp];
+        float p10 = c[xm], p11 = c[0], p12 = c[xp];
+        float p20 = c[yp * E + xm], p21 = c[yp * E], p22 = c[yp * E + xp];
+        float horz = p02 + 2 * p12 + p22 - p00 - 2 * p10 - p20;
+        float vert = p00 + 2 * p01 + p02 - p20 - 2 * p21 - p22;
+        float grad = sqrtf(horz * horz + vert * vert);
+        float s = f.p1 < 0.5f ? f.p0 * grad + 2.0f * f.p1 * p11 : 2.0f * (1.0f - f.p1) * f.p0 * grad + p11;
+        r = fminf(fmaxf(s, 0.f), 1.f);
+      }
+      out[ry * E + rx] = r;
+    }
+  } else if (f.kind == 0) {
+    const int size = f.K;
+    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+      int ry = lo + i / n, rx = lo + i % n;
+      float r = 0.f;
+      if (inside(g, ry, rx)) {
+        int x = g.x0 + rx, y = g.y0 + ry;
+        int i0 = max(y - size / 2, 0), i1 = min(y + (size + 1) / 2, g.h);
+        int j0 = max(x - size / 2, 0), j1 = min(x + (size + 1) / 2, g.w);
+        float cnt = 0.f, s = 0.f;
+        for (int yy = i0; yy < i1; ++yy)
+          for (int xx = j0; xx < j1; ++xx) {
+            cnt += 1.0f;
+            s += in[(yy - g.y0) * E + (xx - g.x0)];
+          }
+        float axy = s / cnt, v = in[ry * E + rx];
+        r = axy > 0.01f ? powf(axy, f.p0 - f.p1) * powf(v, f.p1) : 0.0f;
+      }
+      out[ry * E + rx] = r;
+    }
+  } else {
+    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+      int ry = lo + i / n, rx = lo + i % n;
+      out[ry * E + rx] = in[ry * E + rx];
+    }
+  }
+  __syncthreads();
+}
+
+// Runs a filter chain on buf[0] (valid on [eh - H, eh + VT + H)); returns the
+// buffer index holding the result on the tile band [eh, eh + VT).
+__device__ int run_chain(const FilterDev* fl, int nf, int H, float* bufs[3], const Region& g, int eh)
+{
+  int cur = 0, halo = H;
+  for (int s = 0; s < nf; ++s) {
+    const FilterDev& f = fl[s];
+    int nh = halo - f.R;
+    int nxt = cur == 0 ? 1 : 0;
+    apply_stage(f, bufs[cur], bufs[nxt], bufs[2], g, eh - nh, eh + VT + nh);
+    cur = nxt;
+    halo = nh;
+  }
+  return cur;
+}
+
+__device__ __forceinline__ float wsum(float v)
+{
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int N>
+__device__ void bsum(float (&v)[N], float* red)
+{
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < N; ++k) v[k] = wsum(v[k]);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < N; ++k) red[warp * N + k] = v[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    float s = 0.f;
+    for (int j = 0; j < nw; ++j) s += red[j * N + k];
+    v[k] = s;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_view(const SceneDev* __restrict__ sc, Bufs b, double* __restrict__ cost,
+                                              double* __restrict__ view_cost_out)
+{
+  extern __shared__ float smem[];
+  __shared__ int s_tile;
+  __shared__ bool s_last;
+  __shared__ float red[8 * 6];
+  const int E = sc->E, eh = (E - VT) / 2;
+  float* bufs[3] = {smem, smem + E * E, smem + 2 * E * E};
+  float* fdrr = smem + 3 * E * E;        // VT x VT final DRR
+  Moments* msh = (Moments*)smem;          // reused by the merge
+  const int nv = sc->n_views;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(&b.C->fnext, 1);
+    __syncthreads();
+    const int tile = s_tile;
+    __syncthreads();
+    if (tile >= b.C->ftiles) return;
+    const int k = find_iv(b.foff, b.C->n_iv, tile);
+    const IV& r = b.iv[k];
+    const int t = tile - b.foff[k];
+    const int tx0 = (t % r.ftx) * VT, ty0 = (t / r.ftx) * VT;
+    const int v = k % nv;
+    const ViewDev& V = sc->views[v];
+    Region g{tx0 - eh, ty0 - eh, E, r.w, r.h};
+    const float* drr = b.drr + r.pix;
+    // ---- DRR chain
+    {
+      const int lo = eh - V.h_drr, n = VT + 2 * V.h_drr;
+      for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+        int ry = lo + i / n, rx = lo + i % n;
+        bufs[0][ry * E + rx] = inside(g, ry, rx) ? __ldg(drr + (long long)(g.y0 + ry) * r.w + g.x0 + rx) : 0.f;
+      }
+      __syncthreads();
+      int res = run_chain(V.fdrr, V.n_drr, V.h_drr, bufs, g, eh);
+      for (int i = threadIdx.x; i < VT * VT; i += blockDim.x)
+        fdrr[i] = bufs[res][(eh + i / VT) * E + eh + i % VT];
+      __syncthreads();
+    }
+    // ---- radiograph crop and its chain
+    int rres;
+    {
+      const int lo = eh - V.h_rad, n = VT + 2 * V.h_rad;
+      for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
+        int ry = lo + i / n, rx = lo + i % n;
+        float val = 0.f, s, tt;
+        if (inside(g, ry, rx) && image_coords(V.ipf, r.vp, g.x0 + rx, g.y0 + ry, r.w, r.h, s, tt))
+          val = 1.0f - bilinear(V.rad, V.rad_bps, V.rad_w, V.rad_h, s, tt);
+        bufs[0][ry * E + rx] = val;
+      }
+      __syncthreads();
+      rres = run_chain(V.frad, V.n_rad, V.h_rad, bufs, g, eh);
+    }
+    // ---- masks and moments (Tracker.cpp:744-770)
+    const unsigned n = (unsigned)r.w * (unsigned)r.h;
+    const bool tree = sc->coverage == ASC_SUM_TREE;
+    float fv[4], gv[4];
+    unsigned flags = 0;
+    float s[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int i = threadIdx.x + q * 256;
+      int ly = i / VT, lx = i % VT, x = tx0 + lx, y = ty0 + ly;
+      fv[q] = gv[q] = 0.f;
+      if (x < r.w && y < r.h && (!tree || tree_keep((unsigned)(y * r.w + x), n))) {
+        float d = fdrr[i], gg = bufs[rres][(eh + ly) * E + eh + lx];
+        float bg = 1.0f;
+        if (V.bg && V.bg_thr >= 0.f) {
+          float ss, tt;
+          bg = image_coords(V.ipf, r.vp, x, y, r.w, r.h, ss, tt)
+                 ? (V.bg_thr <= bilinear(V.bg, 32, V.bg_w, V.bg_h, ss, tt) ? 1.0f : 0.0f)
+                 : 0.0f;
+        }
+        float m = bg * (d != 0.0f ? 1.0f : 0.0f);
+        float f = d * m, gm = gg * m;
+        fv[q] = f;
+        gv[q] = gm;
+        flags |= 1u << q;
+        s[0] += m;
+        s[1] += f;
+        s[2] += gm;
+        if (m > 0.5f) {
+          flags |= 1u << (8 + q);
+          s[3] += 1.f;
+          s[4] += f;
+          s[5] += gm;
+        }
+      }
+    }
+    bsum<6>(s, red);
+    const float cnt = s[3], mf = cnt > 0 ? s[4] / cnt : 0.f, mg = cnt > 0 ? s[5] / cnt : 0.f;
+    float c[3] = {0, 0, 0};
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (flags & (1u << (8 + q))) {
+        float a = fv[q] - mf, bb = gv[q] - mg;
+        c[0] = fmaf(a, a, c[0]);
+        c[1] = fmaf(bb, bb, c[1]);
+        c[2] = fmaf(a, bb, c[2]);
+      }
+    bsum<3>(c, red);
+    if (threadIdx.x == 0) {
+      Moments p = {s[0], s[1], s[2], cnt, mf, mg, c[0], c[1], c[2]};
+      b.part[tile] = p;
+      __threadfence();
+      s_last = atomicAdd(&b.ivt[k], 1u) == (unsigned)(r.ftx * r.fty) - 1;
+    }
+    __syncthreads();
+    if (!s_last) continue;
+    __threadfence();
+    // ---- last tile of this view: merge its tiles in FP64
+    const int nt = r.ftx * r.fty, base = b.foff[k];
+    Moments a = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) moments_merge(a, b.part[base + i]);
+    msh[threadIdx.x] = a;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+      if (threadIdx.x < st) moments_merge(msh[threadIdx.x], msh[threadIdx.x + st]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      double vc = 1.0 - moments_ncc(msh[0]);
+      b.vcost[k] = vc;
+      __threadfence();
+      const int item = k / nv;
+      if (atomicAdd(&b.itt[item], 1u) == (unsigned)nv - 1) {
+        __threadfence();
+        finish_item(sc, b, item, cost);
+        if (view_cost_out)
+          for (int j = 0; j < nv; ++j) view_cost_out[item * nv + j] = b.vcost[item * nv + j];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Copies view costs of items finished entirely in k_setup.
+__global__ void k_copy_vcost(const double* vc, double* out, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = vc[i];
+}
+
+// ---------------------------------------------------------------- PSO
+struct Swarm {
+  double* x;    // [bone][particle][6]
+  double* v;
+  double* pbx;
+  double* pbc;
+  double* gx;   // [bone][6]
+  double* gc;   // [bone]
+  int* iter;
+  int* bone;    // item -> bone
+  double* manip;  // item -> x
+};
+
+__device__ __forceinline__ double urand(unsigned long long seed, unsigned long long ctr)
+{
+  unsigned long long z = seed + 0x9e3779b97f4a7c15ull * (ctr + 1);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  z ^= z >> 31;
+  return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+__global__ void k_pso_init(Swarm s, int nb, int np, double lo, double hi, unsigned long long seed)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb * np) return;
+  int p = i % np;
+  for (int d = 0; d < 6; ++d) {
+    double x = p == 0 ? 0.0 : lo + urand(seed, (unsigned long long)i * 6 + d) * (hi - lo);
+    s.x[6 * i + d] = x;
+    s.v[6 * i + d] = 0.0;
+    s.pbx[6 * i + d] = x;
+  }
+  s.pbc[i] = 1e300;
+  if (p == 0) {
+    int b = i / np;
+    for (int d = 0; d < 6; ++d) s.gx[6 * b + d] = 0.0;
+    s.gc[b] = 1e300;
+  }
+  if (i == 0) *s.iter = 0;
+}
+
+// Synchronous velocity/position update (the rule of PSO.cpp:83-109 with
+// runtime w, c1, c2) for every particle of every swarm.
+__global__ void k_pso_update(Swarm s, int nb, int np, double w, double c1, double c2, unsigned long long seed)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb * np) return;
+  int b = i / np;
+  unsigned long long it = (unsigned long long)*s.iter + 1;
+  for (int d = 0; d < 6; ++d) {
+    unsigned long long c = ((it * (unsigned long long)(nb * np) + i) * 6 + d) * 2;
+    double rp = urand(seed, c), rg = urand(seed, c + 1);
+    double x = s.x[6 * i + d];
+    double vv = w * s.v[6 * i + d] + c1 * rp * (s.pbx[6 * i + d] - x) + c2 * rg * (s.gx[6 * b + d] - x);
+    s.v[6 * i + d] = vv;
+    s.x[6 * i + d] = x + vv;
+    s.manip[6 * i + d] = x + vv;
+  }
+  s.bone[i] = b;
+}
+
+// pBest / gBest update after an iteration's costs (one block per swarm).
+__global__ void k_pso_best(Swarm s, int nb, int np, const double* cost)
+{
+  int b = blockIdx.x;
+  __shared__ double bc[256];
+  __shared__ int bi[256];
+  double best = 1e300;
+  int arg = -1;
+  for (int p = threadIdx.x; p < np; p += blockDim.x) {
+    int i = b * np + p;
+    double c = cost[i];
+    if (c < s.pbc[i]) {
+      s.pbc[i] = c;
+      for (int d = 0; d < 6; ++d) s.pbx[6 * i + d] = s.x[6 * i + d];
+    }
+    if (c < best || (c == best && arg >= 0 && p < arg)) {
+      best = c;
+      arg = p;
+    }
+  }
+  bc[threadIdx.x] = best;
+  bi[threadIdx.x] = arg;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      double o = bc[threadIdx.x + st];
+      int oi = bi[threadIdx.x + st];
+      if (o < bc[threadIdx.x] || (o == bc[threadIdx.x] && oi >= 0 && (bi[threadIdx.x] < 0 || oi < bi[threadIdx.x]))) {
+        bc[threadIdx.x] = o;
+        bi[threadIdx.x] = oi;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (bi[0] >= 0 && bc[0] < s.gc[b]) {
+      s.gc[b] = bc[0];
+      for (int d = 0; d < 6; ++d) s.gx[6 * b + d] = s.x[6 * (b * np + bi[0]) + d];
+    }
+    if (b == 0) *s.iter += 1;
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+
+struct asc_engine_s {
+  SceneDev host;
+  SceneDev* dev = nullptr;
+  int max_items = 0, n_views = 0, n_bones = 0;
+  Bufs b{};
+  size_t smem = 0;
+  int sms = 152;
+  bool prof = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  int* d_bone = nullptr;
+  double* d_manip = nullptr;
+  double* d_cost = nullptr;
+  double* d_vcost = nullptr;
+  // plain per-pose path: the reference's Tracker buffers (Tracker.cpp:292-298)
+  std::vector<asc_view_desc> vdesc;
+  std::vector<asc_bone_desc> bdesc;
+  float *p_drr = nullptr, *p_rad = nullptr, *p_mask = nullptr, *p_bg = nullptr, *p_tmp = nullptr, *p_bgr = nullptr;
+  double* p_res = nullptr;
+  std::vector<void*> allocs;
+  ~asc_engine_s()
+  {
+    for (void* p : allocs) cudaFree(p);
+    for (cudaEvent_t x : ev)
+      if (x) cudaEventDestroy(x);
+  }
+  template <class T>
+  cudaError_t alloc(T*& p, size_t n)
+  {
+    cudaError_t e = cudaMalloc((void**)&p, std::max<size_t>(n, 1) * sizeof(T));
+    if (e == cudaSuccess) allocs.push_back((void*)p);
+    return e;
+  }
+};
+
+static int prep_filters(const asc_filter_desc* in, int n, FilterDev* out, int* halo)
+{
+  if (n < 0 || n > MAX_FILTERS) return ASC_ERR_RANGE;
+  int H = 0, m = 0;
+  for (int i = 0; i < n; ++i) {
+    const asc_filter_desc& f = in[i];
+    if (!f.enabled) continue;  // View::filter copies through a disabled filter
+    FilterDev d;
+    memset(&d, 0, sizeof d);
+    d.kind = f.kind;
+    d.p0 = f.p0;
+    d.p1 = f.p1;
+    d.p2 = f.p2;
+    if (f.kind == 1) {
+      d.K = 3;
+      d.R = 1;
+    } else if (f.kind == 0) {
+      d.K = (int)f.p2;
+      if (d.K < 1) return ASC_ERR_ARG;
+      d.R = std::max(d.K / 2, (d.K - 1) / 2);
+    } else if (f.kind == 3 || f.kind == 4) {
+      d.K = gauss_1d(f.p0, d.g, 32);
+      if (d.K < 0) return ASC_ERR_RANGE;
+      if (d.K == 1) continue;  // identity
+      if (f.kind == 4) d.p1 = f.p1 < 1 ? 1 : f.p1;
+      d.R = d.K / 2;
+    } else {
+      return ASC_ERR_ARG;
+    }
+    out[m++] = d;
+    H += d.R;
+  }
+  *halo = H;
+  return m;
+}
+
+static int fill_view(ViewDev& d, const asc_view_desc& v)
+{
+  memcpy(d.cam, v.frame, sizeof d.cam);
+  frame_inverse(v.frame, d.cam_inv);
+  memcpy(d.ip, v.image_plane, sizeof d.ip);
+  memcpy(d.cvp, v.viewport, sizeof d.cvp);
+  for (int j = 0; j < 4; ++j) d.ipf[j] = (float)v.viewport[j];
+  if (!v.radiograph) return ASC_ERR_ARG;
+  int bps;
+  d.rad = image_data(v.radiograph, &d.rad_w, &d.rad_h, &bps);
+  d.rad_bps = bps;
+  if (bps == 32) return ASC_ERR_ARG;
+  d.bg = nullptr;
+  d.bg_thr = v.bg_threshold;
+  if (v.background) {
+    d.bg = (const float*)image_data(v.background, &d.bg_w, &d.bg_h, &bps);
+    if (bps != 32) return ASC_ERR_ARG;
+  }
+  int n = prep_filters(v.drr_filters, v.n_drr_filters, d.fdrr, &d.h_drr);
+  if (n < 0) return n;
+  d.n_drr = n;
+  n = prep_filters(v.rad_filters, v.n_rad_filters, d.frad, &d.h_rad);
+  if (n < 0) return n;
+  d.n_rad = n;
+  return ASC_OK;
+}
+
+static void set_base(BoneDev& B, const double* xyzypr) { memcpy(B.base, xyzypr, sizeof B.base); }
+
+ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bones, const asc_bone_desc* bones,
+                              int rw, int rh, int max_items, int coverage, int cf_model, asc_engine* out)
+{
+  if (!views || !bones || !out || n_views < 1 || n_views > MAX_VIEWS || n_bones < 1 || n_bones > MAX_BONES ||
+      rw < 1 || rh < 1 || max_items < 1 || (coverage != ASC_SUM_TREE && coverage != ASC_SUM_FULL))
+    return ASC_ERR_ARG;
+  if (cf_model != 0) return ASC_ERR_ARG;  // the engine scores NCC; SAD runs through asc_hdist
+  auto* e = new asc_engine_s();
+  SceneDev& S = e->host;
+  memset(&S, 0, sizeof S);
+  S.n_views = n_views;
+  S.n_bones = n_bones;
+  S.rw = rw;
+  S.rh = rh;
+  S.coverage = coverage;
+  int hmax = 0;
+  for (int v = 0; v < n_views; ++v) {
+    int rc = fill_view(S.views[v], views[v]);
+    if (rc) {
+      delete e;
+      return rc;
+    }
+    hmax = std::max(hmax, std::max(S.views[v].h_drr, S.views[v].h_rad));
+  }
+  S.E = VT + 2 * hmax;
+  if (S.E > 120) {
+    delete e;
+    return ASC_ERR_RANGE;
+  }
+  for (int i = 0; i < n_bones; ++i) {
+    auto* vh = (asc_volume_host*)bones[i].volume;
+    if (!vh) {
+      delete e;
+      return ASC_ERR_ARG;
+    }
+    BoneDev& B = S.bones[i];
+    B.vol = vh->dev;
+    memcpy(B.inv_scale, vh->inv_scale, sizeof B.inv_scale);
+    memcpy(B.inv_trans, vh->inv_trans, sizeof B.inv_trans);
+    memcpy(B.pivot, bones[i].pivot, sizeof B.pivot);
+    frame_inverse(B.pivot, B.pivot_inv);
+    set_base(B, bones[i].base_pose);
+    for (int v = 0; v < n_views; ++v) {
+      B.step[v] = bones[i].step[v];
+      B.scale[v] = bones[i].step[v] * vh->dev.norm / bones[i].intensity[v];
+      B.cutoff_raw[v] = bones[i].cutoff[v] / vh->dev.norm;
+    }
+  }
+  e->max_items = max_items;
+  e->n_views = n_views;
+  e->n_bones = n_bones;
+  size_t n_iv = (size_t)max_items * n_views;
+  size_t tiles = (size_t)((rw + VT - 1) / VT) * ((rh + VT - 1) / VT);
+  cudaError_t err = e->alloc(e->dev, 1);
+  if (!err) err = e->alloc(e->b.iv, n_iv);
+  if (!err) err = e->alloc(e->b.roff, n_iv + 1);
+  if (!err) err = e->alloc(e->b.foff, n_iv + 1);
+  if (!err) err = e->alloc(e->b.drr, n_iv * (size_t)rw * rh);
+  if (!err) err = e->alloc(e->b.part, n_iv * tiles);
+  if (!err) err = e->alloc(e->b.vcost, n_iv);
+  if (!err) err = e->alloc(e->b.ivt, n_iv);
+  if (!err) err = e->alloc(e->b.itt, (size_t)max_items);
+  if (!err) err = e->alloc(e->b.C, 1);
+  if (!err) err = e->alloc(e->d_bone, (size_t)max_items);
+  if (!err) err = e->alloc(e->d_manip, (size_t)max_items * 6);
+  if (!err) err = e->alloc(e->d_cost, (size_t)max_items);
+  if (!err) err = e->alloc(e->d_vcost, n_iv);
+  const size_t npix = (size_t)rw * rh;
+  if (!err) err = e->alloc(e->p_drr, npix);
+  if (!err) err = e->alloc(e->p_rad, npix);
+  if (!err) err = e->alloc(e->p_mask, npix);
+  if (!err) err = e->alloc(e->p_bg, npix);
+  if (!err) err = e->alloc(e->p_tmp, npix);
+  if (!err) err = e->alloc(e->p_bgr, npix);
+  if (!err) err = e->alloc(e->p_res, 1);
+  if (!err) err = cudaMemcpy(e->dev, &S, sizeof S, cudaMemcpyHostToDevice);
+  if (!err) err = cudaMemset(e->b.C, 0, sizeof(Counters));
+  if (err) {
+    delete e;
+    return cuda_status(err);
+  }
+  e->vdesc.assign(views, views + n_views);
+  e->bdesc.assign(bones, bones + n_bones);
+  if (asc_fill(e->p_bg, npix, 1.0f, nullptr) || cudaDeviceSynchronize()) {
+    delete e;
+    return ASC_ERR_CUDA;
+  }
+  e->smem = (size_t)(3 * S.E * S.E + VT * VT) * sizeof(float);
+  e->smem = std::max(e->smem, (size_t)256 * sizeof(Moments));
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, dev);
+  err = cudaFuncSetAttribute(k_view, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem);
+  if (err) {
+    delete e;
+    return cuda_status(err);
+  }
+  *out = e;
+  return ASC_OK;
+}
+
+ASC_API int asc_engine_destroy(asc_engine e)
+{
+  if (!e) return ASC_ERR_ARG;
+  cudaDeviceSynchronize();
+  delete e;
+  return ASC_OK;
+}
+
+ASC_API int asc_engine_set_base_pose(asc_engine e, int bone, const double xyzypr[6])
+{
+  if (!e || !xyzypr || bone < 0 || bone >= e->n_bones) return ASC_ERR_ARG;
+  set_base(e->host.bones[bone], xyzypr);
+  ASC_CUDA(cudaMemcpy(&e->dev->bones[bone].base, xyzypr, 6 * sizeof(double), cudaMemcpyHostToDevice));
+  return ASC_OK;
+}
+
+ASC_API int asc_engine_set_radiograph(asc_engine e, int view, asc_image rad)
+{
+  if (!e || !rad || view < 0 || view >= e->n_views) return ASC_ERR_ARG;
+  ViewDev& d = e->host.views[view];
+  int bps;
+  d.rad = image_data(rad, &d.rad_w, &d.rad_h, &bps);
+  if (bps == 32) return ASC_ERR_ARG;
+  d.rad_bps = bps;
+  ASC_CUDA(cudaMemcpy(&e->dev->views[view], &d, sizeof d, cudaMemcpyHostToDevice));
+  return ASC_OK;
+}
+
+static int engine_launch(asc_engine e, int n, const int* bone, const double* manip, double* cost, double* vcost,
+                         cudaStream_t s, bool capturing = false)
+{
+  const bool prof = e->prof && !capturing;
+  if (prof) ASC_CUDA(cudaEventRecord(e->ev[0], s));
+  k_setup<<<1, 1024, 0, s>>>(e->dev, n, bone, manip, e->b, cost, vcost);
+  if (prof) ASC_CUDA(cudaEventRecord(e->ev[1], s));
+  k_ray<<<e->sms * 8, 256, 0, s>>>(e->dev, e->b);
+  if (prof) ASC_CUDA(cudaEventRecord(e->ev[2], s));
+  k_view<<<e->sms * 4, 256, e->smem, s>>>(e->dev, e->b, cost, vcost);
+  if (prof) ASC_CUDA(cudaEventRecord(e->ev[3], s));
+  if (vcost) k_copy_vcost<<<8, 256, 0, s>>>(e->b.vcost, vcost, n * e->n_views);
+  ASC_LAUNCH_CHECK();
+  return ASC_OK;
+}
+
+ASC_API int asc_engine_profile(asc_engine e, int enable)
+{
+  if (!e) return ASC_ERR_ARG;
+  if (enable && !e->ev[0])
+    for (int i = 0; i < 4; ++i) ASC_CUDA(cudaEventCreate(&e->ev[i]));
+  e->prof = enable != 0;
+  return ASC_OK;
+}
+
+ASC_API int asc_engine_stats(asc_engine e, float ms[3], unsigned long long* samples, unsigned long long* pixels)
+{
+  if (!e) return ASC_ERR_ARG;
+  if (ms) {
+    if (!e->ev[0]) return ASC_ERR_STATE;
+    ASC_CUDA(cudaEventSynchronize(e->ev[3]));
+    for (int i = 0; i < 3; ++i) ASC_CUDA(cudaEventElapsedTime(&ms[i], e->ev[i], e->ev[i + 1]));
+  }
+  Counters C;
+  ASC_CUDA(cudaMemcpy(&C, e->b.C, sizeof C, cudaMemcpyDeviceToHost));
+  if (samples) *samples = C.samples;
+  if (pixels) *pixels = C.pixels;
+  return ASC_OK;
+}
+
+ASC_API int asc_engine_eval(asc_engine e, int n, const int* bone, const double* manip, double* cost, double* vcost,
+                            void* stream)
+{
+  if (!e || !bone || !manip || !cost || n < 1 || n > e->max_items) return ASC_ERR_ARG;
+  return engine_launch(e, n, bone, manip, cost, vcost, S(stream));
+}
+
+ASC_API int asc_engine_eval_host(asc_engine e, int n, const int* bone, const double* manip, double* cost,
+                                 double* vcost, void* stream)
+{
+  if (!e || !bone || !manip || !cost || n < 1 || n > e->max_items) return ASC_ERR_ARG;
+  cudaStream_t s = S(stream);
+  ASC_CUDA(cudaMemcpyAsync(e->d_bone, bone, n * sizeof(int), cudaMemcpyHostToDevice, s));
+  ASC_CUDA(cudaMemcpyAsync(e->d_manip, manip, n * 6 * sizeof(double), cudaMemcpyHostToDevice, s));
+  int rc = engine_launch(e, n, e->d_bone, e->d_manip, e->d_cost, vcost ? e->d_vcost : nullptr, s);
+  if (rc) return rc;
+  ASC_CUDA(cudaMemcpyAsync(cost, e->d_cost, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (vcost)
+    ASC_CUDA(cudaMemcpyAsync(vcost, e->d_vcost, (size_t)n * e->n_views * sizeof(double), cudaMemcpyDeviceToHost, s));
+  Counters C;
+  ASC_CUDA(cudaMemcpyAsync(&C, e->b.C, sizeof C, cudaMemcpyDeviceToHost, s));
+  ASC_CUDA(cudaStreamSynchronize(s));
+  return C.error ? C.error : ASC_OK;
+}
+
+ASC_API int asc_engine_debug(asc_engine e, const float** drr, const int** layout)
+{
+  if (!e) return ASC_ERR_ARG;
+  if (drr) *drr = e->b.drr;
+  if (layout) *layout = (const int*)e->b.iv;
+  return ASC_OK;
+}
+
+ASC_API int asc_engine_pso(asc_engine e, int np, int n_iter, double w, double c1, double c2, double lo, double hi,
+                           uint64_t seed, double* best_manip, double* best_cost, long long* evals, void* stream)
+{
+  if (!e || np < 1 || n_iter < 1 || !best_manip || !best_cost) return ASC_ERR_ARG;
+  const int nb = e->n_bones, n = nb * np;
+  if (n > e->max_items) return ASC_ERR_RANGE;
+  cudaStream_t s = S(stream);
+  bool own = false;
+  if (!s) {
+    ASC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    own = true;
+  }
+  Swarm sw;
+  double* buf = nullptr;
+  int* ibuf = nullptr;
+  size_t nd = (size_t)n * 6 * 3 + n + nb * 6 + nb;
+  cudaError_t err = cudaMalloc(&buf, nd * sizeof(double));
+  if (!err) err = cudaMalloc(&ibuf, sizeof(int));
+  if (err) {
+    if (buf) cudaFree(buf);
+    if (own) cudaStreamDestroy(s);
+    return cuda_status(err);
+  }
+  sw.x = buf;
+  sw.v = sw.x + (size_t)n * 6;
+  sw.pbx = sw.v + (size_t)n * 6;
+  sw.pbc = sw.pbx + (size_t)n * 6;
+  sw.gx = sw.pbc + n;
+  sw.gc = sw.gx + nb * 6;
+  sw.iter = ibuf;
+  sw.bone = e->d_bone;
+  sw.manip = e->d_manip;
+  int rc = ASC_OK;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int tb = 128, gb = (n + tb - 1) / tb;
+  k_pso_init<<<gb, tb, 0, s>>>(sw, nb, np, lo, hi, seed);
+  err = cudaGetLastError();
+  if (!err) err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (!err) {
+    k_pso_update<<<gb, tb, 0, s>>>(sw, nb, np, w, c1, c2, seed);
+    engine_launch(e, n, e->d_bone, e->d_manip, e->d_cost, nullptr, s, true);
+    k_pso_best<<<nb, 256, 0, s>>>(sw, nb, np, e->d_cost);
+    err = cudaStreamEndCapture(s, &graph);
+  }
+  if (!err) err = cudaGraphInstantiate(&exec, graph, 0);
+  for (int it = 0; !err && it < n_iter; ++it) err = cudaGraphLaunch(exec, s);
+  if (!err) err = cudaMemcpyAsync(best_manip, sw.gx, nb * 6 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (!err) err = cudaMemcpyAsync(best_cost, sw.gc, nb * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (!err) err = cudaStreamSynchronize(s);
+  if (err) rc = cuda_status(err);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  cudaFree(buf);
+  cudaFree(ibuf);
+  if (own) cudaStreamDestroy(s);
+  if (evals) *evals = (long long)n * n_iter;
+  return rc;
+}
+
+// ---------------------------------------------------------------- plain path
+// Tracker::trackFrame (Tracker.cpp:583-773) one pose at a time over the plain
+// per-operator kernels: the same launch sequence as the reference (ray cast,
+// DRR filters, radiograph crop, radiograph filters, masks, three multiplies,
+// NCC) with the NCC read back to the host after every view.  This is the
+// drop-in form the batched engine is measured against.
+static int chain_plain(const asc_filter_desc* fl, int nf, float*& cur, float*& other, int w, int h, cudaStream_t s)
+{
+  for (int i = 0; i < nf; ++i) {
+    if (fl[i].enabled) {
+      int rc = launch_filter(fl[i], cur, other, w, h, s);
+      if (rc) return rc;
+      std::swap(cur, other);
+    }
+  }
+  return ASC_OK;
+}
+
+ASC_API int asc_engine_eval_plain(asc_engine e, int n, const int* bone, const double* manip, double* cost,
+                                  double* view_cost, void* stream)
+{
+  if (!e || !bone || !manip || !cost || n < 1) return ASC_ERR_ARG;
+  cudaStream_t s = S(stream);
+  const SceneDev& S_ = e->host;
+  const int nv = e->n_views;
+  for (int it = 0; it < n; ++it) {
+    int bi = bone[it];
+    if (bi < 0 || bi >= e->n_bones) return ASC_ERR_ARG;
+    const BoneDev& B = S_.bones[bi];
+    const asc_bone_desc& BD = e->bdesc[bi];
+    double base[12], man[12], t1[12], t2[12], xyz[6];
+    frame_from_xyzypr(B.base, base);
+    frame_from_axis_angle(manip + 6 * it, man);
+    frame_mul(base, B.pivot_inv, t1);
+    frame_mul(t1, man, t2);
+    frame_mul(t2, B.pivot, t1);
+    frame_to_xyzypr(t1, xyz);
+    frame_from_xyzypr(xyz, t1);
+    double total = 0.0;
+    for (int v = 0; v < nv; ++v) {
+      const ViewDev& V = S_.views[v];
+      const asc_view_desc& VD = e->vdesc[v];
+      double mv[12], imv[12], imv16[16], vp[4];
+      float m[12];
+      frame_mul(V.cam_inv, t1, mv);
+      frame_inverse(mv, imv);
+      frame_row_matrix(imv, imv16);
+      fold_matrix(imv16, B.inv_scale, B.inv_trans, m);
+      double vc;
+      if (!calculate_viewport(mv, V.cam, V.ip, B.inv_scale, B.inv_trans, vp)) {
+        vc = 9999.0;
+      } else {
+        double fw = vp[2] * S_.rw / V.cvp[2], fh = vp[3] * S_.rh / V.cvp[3];
+        unsigned w = fw > 0 ? (unsigned)fw : 0u, h = fh > 0 ? (unsigned)fh : 0u;
+        if (w > (unsigned)S_.rw || h > (unsigned)S_.rh) return ASC_ERR_RANGE;
+        if (w == 0 || h == 0) {
+          vc = 1.0 - 1e5;
+        } else {
+          float vpf[4] = {(float)vp[0], (float)vp[1], (float)vp[2], (float)vp[3]};
+          int rc = raycast_launch(B.vol, m, vpf, BD.step[v], BD.intensity[v], BD.cutoff[v], e->p_drr, w, h, s);
+          float *d = e->p_drr, *o = e->p_tmp;
+          if (!rc) rc = chain_plain(VD.drr_filters, VD.n_drr_filters, d, o, w, h, s);
+          // the DRR chain ping-pongs p_drr/p_tmp and leaves one of them free (o);
+          // the radiograph chain ping-pongs p_rad/o; p_mask stays free
+          if (!rc) rc = asc_rad_render(VD.radiograph, V.ipf, vpf, e->p_rad, w, h, s);
+          float *r = e->p_rad, *ro = o;
+          if (!rc) rc = chain_plain(VD.rad_filters, VD.n_rad_filters, r, ro, w, h, s);
+          float* mask = e->p_mask;
+          float* bgm = e->p_bg;  // all ones: the mask of a disabled background
+          if (!rc && VD.background && VD.bg_threshold >= 0) {
+            bgm = e->p_bgr;
+            rc = asc_background_render(VD.background, V.ipf, vpf, VD.bg_threshold, bgm, w, h, s);
+          }
+          if (!rc) rc = asc_drr_background(d, mask, w, h, s);
+          if (!rc) rc = asc_multiply(bgm, mask, mask, w, h, s);
+          if (!rc) rc = asc_multiply(r, mask, r, w, h, s);
+          if (!rc) rc = asc_multiply(d, mask, d, w, h, s);
+          double ncc = 0;
+          if (!rc) rc = asc_ncc(d, r, mask, w * h, S_.coverage, e->p_res, s);
+          if (!rc) {
+            cudaError_t err = cudaMemcpyAsync(&ncc, e->p_res, sizeof(double), cudaMemcpyDeviceToHost, s);
+            if (!err) err = cudaStreamSynchronize(s);
+            if (err) rc = cuda_status(err);
+          }
+          if (rc) return rc;
+          vc = 1.0 - ncc;
+        }
+      }
+      if (view_cost) view_cost[it * nv + v] = vc;
+      total += vc;
+    }
+    cost[it] = total < 0 ? 9999.0 : total;
+  }
+  return ASC_OK;
+}

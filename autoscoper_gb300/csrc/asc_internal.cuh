@@ -1,0 +1,430 @@
+// Internal declarations shared by the CUDA translation units of
+// libautoscoper_gb300.so: status handling, the device volume layout, the
+// FP32 ray march, FP64 rigid-frame algebra (host and device), and the
+// reduction helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "../../include/autoscoper_gb300.h"
+
+#define ASC_API extern "C" __attribute__((visibility("default")))
+
+namespace asc {
+
+void set_cuda_error(cudaError_t e);
+int cuda_status(cudaError_t e);
+inline cudaStream_t S(void* s) { return (cudaStream_t)s; }
+
+#define ASC_CUDA(call)                            \
+  do {                                            \
+    cudaError_t e_ = (call);                      \
+    if (e_ != cudaSuccess) return cuda_status(e_); \
+  } while (0)
+
+#define ASC_LAUNCH_CHECK() ASC_CUDA(cudaGetLastError())
+
+// --------------------------------------------------------------------------
+// Device volume.  Voxels are stored "x-paired": word (x, y, z) holds voxel
+// x in its low half and voxel min(x+1, nx-1) in its high half, so that one
+// 32-bit load fetches both x taps of a trilinear sample.  The halves are u16
+// integers (ASC_STORE_U16), IEEE half (ASC_STORE_F16) or bfloat16
+// (ASC_STORE_BF16), all holding the stored integer value; `norm` (1/65535
+// or 1/255) turns a raw value into the normalized float that
+// cudaReadModeNormalizedFloat would return.
+// --------------------------------------------------------------------------
+struct DevVolume {
+  const uint32_t* pairs;  // nz * ny * nx words
+  int nx, ny, nz;
+  int storage;
+  float norm;
+};
+
+struct asc_volume_host {
+  DevVolume dev;
+  uint32_t* pairs;
+  float inv_scale[3], inv_trans[3];
+  double trans_center[3];
+  float min_value, max_value;
+  int dims[3];
+  int bps;
+};
+
+template <int STORE>
+__device__ __forceinline__ void unpack(uint32_t w, float& lo, float& hi)
+{
+  if (STORE == ASC_STORE_BF16) {
+    lo = __uint_as_float(w << 16);
+    hi = __uint_as_float(w & 0xffff0000u);
+  } else if (STORE == ASC_STORE_F16) {
+    __half2_raw r;
+    r.x = (unsigned short)(w & 0xffffu);
+    r.y = (unsigned short)(w >> 16);
+    float2 f = __half22float2(*reinterpret_cast<__half2*>(&r));
+    lo = f.x;
+    hi = f.y;
+  } else {
+    // u16 -> float without a conversion unit: 2^23 + v is exact in FP32.
+    lo = __uint_as_float(0x4b000000u | (w & 0xffffu)) - 8388608.0f;
+    hi = __uint_as_float(0x4b000000u | (w >> 16)) - 8388608.0f;
+  }
+}
+
+// Index and weight of the lower tap of a linear filter at voxel coordinate
+// X (texel centres at integers): k = nearest integer to X - 0.5, a = X - k in
+// [0, 1].  Where X is an integer the tie may give k = floor(X) - 1 with
+// a = 1, which selects the same value.
+__device__ __forceinline__ void tap(float X, int& k, float& a)
+{
+  const float M = 12582912.0f;  // 1.5 * 2^23
+  float t = __fadd_rn(__fadd_rn(X, -0.5f), M);
+  k = __float_as_int(t) - 0x4b400000;
+  a = __fadd_rn(X, -__fadd_rn(t, -M));
+}
+
+// One ray of cuda_volume_render_kernel (RayCaster_kernels.cu:144-195) from
+// t = far down to t > near in unit steps, sampling at voxel coordinates
+// (X0 + t dX, Y0 + t dY, Z0 + t dZ).  Returns the sum of raw samples above
+// cutoff_raw (the caller scales by step * norm / intensity).
+template <int STORE>
+__device__ __forceinline__ float march(const DevVolume& V, float X0, float dX, float Y0, float dY, float Z0, float dZ,
+                                       float tnear, float tfar, float cutoff_raw)
+{
+  const uint32_t* __restrict__ P = V.pairs;
+  const int nx = V.nx, ny = V.ny, nz = V.nz;
+  const int sxy = nx * ny;
+  float acc = 0.f;
+  for (float t = tfar; t > tnear; t -= 1.0f) {
+    int ix, iy, iz;
+    float ax, ay, az;
+    tap(fmaf(t, dX, X0), ix, ax);
+    tap(fmaf(t, dY, Y0), iy, ay);
+    tap(fmaf(t, dZ, Z0), iz, az);
+    // clamp-to-edge; below the first texel both taps are texel 0
+    if (ix < 0) { ix = 0; ax = 0.f; }
+    ix = min(ix, nx - 1);
+    int y0 = max(iy, 0), y1 = min(iy + 1, ny - 1);
+    y0 = min(y0, ny - 1);
+    y1 = max(y1, 0);
+    int z0 = max(iz, 0), z1 = min(iz + 1, nz - 1);
+    z0 = min(z0, nz - 1);
+    z1 = max(z1, 0);
+    const int r00 = z0 * sxy + y0 * nx + ix;
+    const int r10 = z0 * sxy + y1 * nx + ix;
+    const int r01 = z1 * sxy + y0 * nx + ix;
+    const int r11 = z1 * sxy + y1 * nx + ix;
+    uint32_t w00 = __ldg(P + r00), w10 = __ldg(P + r10), w01 = __ldg(P + r01), w11 = __ldg(P + r11);
+    float a0, a1, b0, b1, c0, c1, d0, d1;
+    unpack<STORE>(w00, a0, a1);
+    unpack<STORE>(w10, b0, b1);
+    unpack<STORE>(w01, c0, c1);
+    unpack<STORE>(w11, d0, d1);
+    float e00 = fmaf(ax, a1 - a0, a0);
+    float e10 = fmaf(ax, b1 - b0, b0);
+    float e01 = fmaf(ax, c1 - c0, c0);
+    float e11 = fmaf(ax, d1 - d0, d0);
+    float f0 = fmaf(ay, e10 - e00, e00);
+    float f1 = fmaf(ay, e11 - e01, e01);
+    float s = fmaf(az, f1 - f0, f0);
+    acc += s > cutoff_raw ? s : 0.f;
+  }
+  return acc;
+}
+
+// Per-ray set-up of cuda_volume_render_kernel: pixel (x, y) of a w x h image
+// over `vp`, camera->volume matrix m (3x4 row-major, normalisation folded).
+// Returns false when the ray misses the unit box [0,1]x[0,1]x[-1,0].
+struct RaySetup {
+  float X0, dX, Y0, dY, Z0, dZ, tnear, tfar;
+};
+
+__device__ __forceinline__ bool ray_setup(const float* m, const float* vp, int x, int y, int w, int h, float step,
+                                          int nx, int ny, int nz, RaySetup& r)
+{
+  float u = vp[0] + vp[2] * (x / (float)w);
+  float v = vp[1] + vp[3] * (y / (float)h);
+  float inv = step / sqrtf(u * u + v * v + 4.0f);
+  float lx = u * inv, ly = v * inv, lz = -2.0f * inv;
+  float ox = m[3], oy = m[7], oz = m[11];
+  float dx = m[0] * lx + m[1] * ly + m[2] * lz;
+  float dy = m[4] * lx + m[5] * ly + m[6] * lz;
+  float dz = m[8] * lx + m[9] * ly + m[10] * lz;
+  float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
+  float bx = ix * (0.0f - ox), tx = ix * (1.0f - ox);
+  float by = iy * (0.0f - oy), ty = iy * (1.0f - oy);
+  float bz = iz * (-1.0f - oz), tz = iz * (0.0f - oz);
+  float tn = fmaxf(fmaxf(fminf(tx, bx), fminf(ty, by)), fminf(tz, bz));
+  float tf = fminf(fminf(fmaxf(tx, bx), fmaxf(ty, by)), fmaxf(tz, bz));
+  if (!(tf > tn)) return false;
+  // t -= 1 stops making progress at 2^24; the reference would spin forever on
+  // such a degenerate ray, here it counts as a miss.
+  if (!(tf < 8388608.0f)) return false;
+  r.tnear = tn < 0.0f ? 0.0f : tn;
+  r.tfar = tf;
+  // texture coordinates (p.x, 1 - p.y, -p.z) in texel units
+  r.X0 = ox * nx - 0.5f;
+  r.dX = dx * nx;
+  r.Y0 = (1.0f - oy) * ny - 0.5f;
+  r.dY = -dy * ny;
+  r.Z0 = -oz * nz - 0.5f;
+  r.dZ = -dz * nz;
+  return true;
+}
+
+// Bilinear read of an 8/16-bit (normalized) or float image with normalized
+// coordinates and clamp-to-edge, as tex2D<float> with the reference's
+// texture object (cutil_create_tex_obj.h:6-28).
+__device__ __forceinline__ float image_texel(const void* img, int bps, int i)
+{
+  if (bps == 16) return __ldg((const unsigned short*)img + i) * (1.0f / 65535.0f);
+  if (bps == 8) return __ldg((const unsigned char*)img + i) * (1.0f / 255.0f);
+  return __ldg((const float*)img + i);
+}
+
+__device__ __forceinline__ float bilinear(const void* img, int bps, int W, int H, float s, float t)
+{
+  float X = s * W - 0.5f, Y = t * H - 0.5f;
+  float fx = floorf(X), fy = floorf(Y);
+  float ax = X - fx, ay = Y - fy;
+  fx = fminf(fmaxf(fx, -1.0f), (float)W);
+  fy = fminf(fmaxf(fy, -1.0f), (float)H);
+  int x0 = (int)fx, y0 = (int)fy;
+  int xa = min(max(x0, 0), W - 1), xb = min(max(x0 + 1, 0), W - 1);
+  int ya = min(max(y0, 0), H - 1), yb = min(max(y0 + 1, 0), H - 1);
+  float v00 = image_texel(img, bps, ya * W + xa), v01 = image_texel(img, bps, ya * W + xb);
+  float v10 = image_texel(img, bps, yb * W + xa), v11 = image_texel(img, bps, yb * W + xb);
+  float r0 = fmaf(ax, v01 - v00, v00), r1 = fmaf(ax, v11 - v10, v10);
+  return fmaf(ay, r1 - r0, r0);
+}
+
+// Film-plane pixel of RadRenderer/BackgroundRenderer (RadRenderer_kernels.cu:103-107).
+__device__ __forceinline__ bool image_coords(const float* ip, const float* vp, int x, int y, int w, int h, float& s,
+                                             float& t)
+{
+  float u = vp[0] + vp[2] * (x / (float)w);
+  float v = vp[1] + vp[3] * (y / (float)h);
+  s = (u - ip[0]) / ip[2] + 0.5f;
+  t = 0.5f - (v - ip[1]) / ip[3];
+  return !(s < 0.0f || t < 0.0f || s > 1.0f || t > 1.0f);
+}
+
+// Whether element i of n reaches the reference's multi-level sum()
+// (Ncc_kernels.cu:151-187): levels of T = min(n_l, 256) threads fold shared
+// memory with s = T/2, T/4, ..., never reading slots at or above 2s.
+__host__ __device__ __forceinline__ bool tree_keep(unsigned i, unsigned n)
+{
+  unsigned idx = i;
+  while (n > 1) {
+    unsigned T = n < 256u ? n : 256u;
+    if (T & (T - 1)) {
+      unsigned t = idx % T;
+      for (unsigned s = T >> 1; s > 0; s >>= 1) {
+        if (t >= 2 * s) return false;
+        if (t >= s) t -= s;
+      }
+    }
+    idx /= T;
+    n = (n + T - 1) / T;
+  }
+  return true;
+}
+
+// Moments of one block or tile for the NCC (combined in FP64 with Chan et
+// al.'s pairwise update): sums over all covered pixels, and count, means and
+// co-moments over the covered pixels whose mask > 0.5.
+struct Moments {
+  double sm, sf, sg;   // sum of mask, f, g over covered pixels
+  double n;            // covered pixels with mask > 0.5
+  double mf, mg;       // their means
+  double cff, cgg, cfg;  // their centred co-moments
+};
+
+__host__ __device__ inline void moments_merge(Moments& a, const Moments& b)
+{
+  a.sm += b.sm;
+  a.sf += b.sf;
+  a.sg += b.sg;
+  double n = a.n + b.n;
+  if (b.n == 0) return;
+  if (a.n == 0) {
+    a.n = b.n; a.mf = b.mf; a.mg = b.mg; a.cff = b.cff; a.cgg = b.cgg; a.cfg = b.cfg;
+    return;
+  }
+  double df = b.mf - a.mf, dg = b.mg - a.mg, k = a.n * b.n / n;
+  a.cff += b.cff + df * df * k;
+  a.cgg += b.cgg + dg * dg * k;
+  a.cfg += b.cfg + df * dg * k;
+  a.mf += df * b.n / n;
+  a.mg += dg * b.n / n;
+  a.n = n;
+}
+
+// gpu::ncc's result from the merged moments (Ncc_kernels.cu:116-134):
+// means over all covered pixels (sum f / sum mask), centred products over
+// mask > 0.5, den < 1e-5 -> 1e5.
+__host__ __device__ inline double moments_ncc(const Moments& m)
+{
+  double mF = m.sf / m.sm, mG = m.sg / m.sm;
+  double ef = m.mf - mF, eg = m.mg - mG;
+  double num = m.cfg + m.n * ef * eg;
+  double d1 = m.cff + m.n * ef * ef;
+  double d2 = m.cgg + m.n * eg * eg;
+  if (m.n == 0) num = d1 = d2 = 0.0;
+  double den = sqrt(d1 * d2);
+  if (!(den >= 1e-5)) return den != den ? den : 1e5;
+  return num / den;
+}
+
+// ---- FP64 rigid frames (CoordFrame.cpp), host and device ----
+__host__ __device__ inline void frame_identity(double* f)
+{
+  for (int i = 0; i < 12; ++i) f[i] = 0.0;
+  f[0] = f[4] = f[8] = 1.0;
+}
+
+__host__ __device__ inline void frame_rotate(double* f, const double* caxis, double angle)
+{
+  const double PI = 3.14159265358979323846;
+  double a0 = caxis[0], a1 = caxis[1], a2 = caxis[2];
+  double c = cos(PI * angle / 180.0), s = sin(PI * angle / 180.0);
+  double mag = sqrt(a0 * a0 + a1 * a1 + a2 * a2);
+  if (mag == 0) return;
+  a0 /= mag; a1 /= mag; a2 /= mag;
+  double oc = 1.0 - c;
+  double R[9] = {oc * a0 * a0 + c,      oc * a0 * a1 + s * a2, oc * a0 * a2 - s * a1,
+                 oc * a0 * a1 - s * a2, oc * a1 * a1 + c,      oc * a1 * a2 + s * a0,
+                 oc * a0 * a2 + s * a1, oc * a1 * a2 - s * a0, oc * a2 * a2 + c};
+  double t[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) t[3 * i + j] = f[3 * i] * R[j] + f[3 * i + 1] * R[3 + j] + f[3 * i + 2] * R[6 + j];
+  for (int i = 0; i < 9; ++i) f[i] = t[i];
+}
+
+__host__ __device__ inline void frame_from_xyzypr(const double* v, double* f)
+{
+  frame_identity(f);
+  double ax[3];
+  ax[0] = f[6]; ax[1] = f[7]; ax[2] = f[8];
+  frame_rotate(f, ax, v[3]);
+  ax[0] = f[3]; ax[1] = f[4]; ax[2] = f[5];
+  frame_rotate(f, ax, v[4]);
+  ax[0] = f[0]; ax[1] = f[1]; ax[2] = f[2];
+  frame_rotate(f, ax, v[5]);
+  f[9] += v[0]; f[10] += v[1]; f[11] += v[2];
+}
+
+__host__ __device__ inline void frame_from_axis_angle(const double* v, double* f)
+{
+  frame_identity(f);
+  double ang = sqrt(v[3] * v[3] + v[4] * v[4] + v[5] * v[5]);
+  if (ang != 0) frame_rotate(f, v + 3, ang);
+  f[9] += v[0]; f[10] += v[1]; f[11] += v[2];
+}
+
+__host__ __device__ inline void frame_to_xyzypr(const double* f, double* v)
+{
+  const double PI = 3.14159265358979323846;
+  v[0] = f[9]; v[1] = f[10]; v[2] = f[11];
+  v[3] = 180.0 * atan2(f[1], f[0]) / PI;
+  v[4] = 180.0 * atan2(-f[2], sqrt(f[5] * f[5] + f[8] * f[8])) / PI;
+  v[5] = 180.0 * atan2(f[5], f[8]) / PI;
+}
+
+__host__ __device__ inline void frame_mul(const double* a, const double* b, double* out)
+{
+  double r[12];
+  for (int c = 0; c < 3; ++c)
+    for (int i = 0; i < 3; ++i) r[3 * c + i] = a[i] * b[3 * c] + a[3 + i] * b[3 * c + 1] + a[6 + i] * b[3 * c + 2];
+  for (int i = 0; i < 3; ++i) r[9 + i] = a[i] * b[9] + a[3 + i] * b[10] + a[6 + i] * b[11] + a[9 + i];
+  for (int i = 0; i < 12; ++i) out[i] = r[i];
+}
+
+__host__ __device__ inline void frame_inverse(const double* a, double* out)
+{
+  double r[12] = {a[0], a[3], a[6], a[1], a[4], a[7], a[2], a[5], a[8], 0, 0, 0};
+  r[9] = -(r[0] * a[9] + r[3] * a[10] + r[6] * a[11]);
+  r[10] = -(r[1] * a[9] + r[4] * a[10] + r[7] * a[11]);
+  r[11] = -(r[2] * a[9] + r[5] * a[10] + r[8] * a[11]);
+  for (int i = 0; i < 12; ++i) out[i] = r[i];
+}
+
+__host__ __device__ inline void frame_point(const double* f, const double* p, double* q)
+{
+  double r0 = f[0] * p[0] + f[3] * p[1] + f[6] * p[2] + f[9];
+  double r1 = f[1] * p[0] + f[4] * p[1] + f[7] * p[2] + f[10];
+  double r2 = f[2] * p[0] + f[5] * p[1] + f[8] * p[2] + f[11];
+  q[0] = r0; q[1] = r1; q[2] = r2;
+}
+
+// RayCaster::setInvModelView (RayCaster.cpp:88-114) applied to the inverse of
+// `modelview`: the 3x4 camera->volume matrix with the volume normalisation
+// folded in, rounded to float as the reference stores it.
+__host__ __device__ inline void fold_matrix(const double* imv16, const float* inv_scale, const float* inv_trans,
+                                            float* m12)
+{
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 4; ++c)
+      m12[4 * r + c] = (float)(imv16[4 * r + c] * (double)inv_scale[r] + imv16[12 + c] * (double)inv_trans[r]);
+}
+
+__host__ __device__ inline void frame_row_matrix(const double* f, double* m)
+{
+  m[0] = f[0]; m[1] = f[3]; m[2] = f[6]; m[3] = f[9];
+  m[4] = f[1]; m[5] = f[4]; m[6] = f[7]; m[7] = f[10];
+  m[8] = f[2]; m[9] = f[5]; m[10] = f[8]; m[11] = f[11];
+  m[12] = 0; m[13] = 0; m[14] = 0; m[15] = 1;
+}
+
+// Tracker::calculate_viewport (Tracker.cpp:923-1032).
+__host__ __device__ inline bool calculate_viewport(const double* mv, const double* cam, const double* ip,
+                                                   const float* inv_scale, const float* inv_trans, double* vp)
+{
+  double mm[4] = {1.0, 1.0, -1.0, -1.0};
+  const double corners[24] = {0, 0, -1, 0, 0, 0, 0, 1, -1, 0, 1, 0, 1, 0, -1, 1, 0, 0, 1, 1, -1, 1, 1, 0};
+  for (int j = 0; j < 8; ++j) {
+    double p[3], q[3];
+    for (int k = 0; k < 3; ++k) p[k] = (corners[3 * j + k] - (double)inv_trans[k]) / (double)inv_scale[k];
+    frame_point(mv, p, q);
+    double fx = -2 * q[0] / q[2], fy = -2 * q[1] / q[2];
+    if (mm[0] > fx) mm[0] = fx;
+    if (mm[1] > fy) mm[1] = fy;
+    if (mm[2] < fx) mm[2] = fx;
+    if (mm[3] < fy) mm[3] = fy;
+  }
+  double ci[12], a[3], b[3];
+  frame_inverse(cam, ci);
+  frame_point(ci, ip + 3, a);
+  frame_point(ci, ip + 9, b);
+  double rf[4] = {-2 * a[0] / a[2], -2 * a[1] / a[2], -2 * b[0] / b[2], -2 * b[1] / b[2]};
+  if (mm[0] > rf[2] && mm[2] > rf[2]) return false;
+  if (mm[1] > rf[3] && mm[3] > rf[3]) return false;
+  if (mm[0] < rf[0] && mm[2] < rf[0]) return false;
+  if (mm[1] < rf[1] && mm[3] < rf[1]) return false;
+  if (mm[0] == 1.0 && mm[1] == 1.0 && mm[2] == -1.0 && mm[3] == -1.0) return false;
+  if (mm[0] < rf[0]) mm[0] = rf[0];
+  if (mm[1] < rf[1]) mm[1] = rf[1];
+  if (mm[2] > rf[2]) mm[2] = rf[2];
+  if (mm[3] > rf[3]) mm[3] = rf[3];
+  vp[0] = mm[0];
+  vp[1] = mm[1];
+  vp[2] = mm[2] - mm[0];
+  vp[3] = mm[3] - mm[1];
+  return true;
+}
+
+// Gaussian weights of GaussianFilter::set_radius / SharpenFilter::makeFilter:
+// K = 2 floor(3r) + 1 taps per axis; the 2-D kernel 2.71828^(-(i^2+j^2)/(2r))
+// normalised to 1 is the outer product of the returned 1-D weights g (sum 1).
+// Returns K (1 = identity).
+int gauss_1d(float radius, float* g, int cap);
+
+// Filter dispatch used by the plain operators and the engine set-up.
+int launch_filter(const asc_filter_desc& f, const float* in, float* out, int w, int h, cudaStream_t s);
+
+// One plain ray-cast launch with an already folded float matrix.
+int raycast_launch(const DevVolume& V, const float* m12, const float* vp, float step, float intensity, float cutoff,
+                   float* out, int w, int h, cudaStream_t s);
+
+}  // namespace asc

@@ -1,0 +1,333 @@
+"""Benchmark of the registration cost path on the batched PSO workload.
+
+Workload (one "step" = one frame registered): 3 bones (uint16 phantoms
+160x96x96, 256x128x128, 200x200x120 at 0.4 mm), 2 views with 1024x1024 uint16
+radiographs, the filter chain Contrast(2.5, 0.9) -> Sharpen(1) -> Gaussian(1.5)
+-> Sobel on both the DRR and the radiograph lists, masked NCC, and a
+synchronous PSO of 100 particles x 50 iterations per bone (w 0.7298,
+c1 = c2 = 1.4962), every iteration scoring all 300 particles of the three
+swarms in one graph-captured launch sequence.  Data are seeded synthetic
+phantoms and radiographs rendered at a seeded ground truth.
+
+Prints one JSON line (see the keys below).  `--impl reference` times the
+CPU restatement of the path (the oracle) on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "pose evals/s (DRR+filter+NCC, 2 views)"
+CONFIG = {"workload": "batched PSO, 3 bones (160x96x96, 256x128x128, 200x200x120 u16 @0.4mm), 2 views, "
+                      "1024x1024 u16 radiographs, Contrast->Sharpen->Gaussian(1.5)->Sobel, masked NCC, "
+                      "100 particles x 50 iterations per bone",
+          "bones": 3, "views": 2, "render": [1024, 1024], "particles": 100, "iterations": 50}
+SHAPES = [(96, 96, 160), (128, 128, 256), (120, 200, 200)]  # (depth, height, width)
+
+
+def make_scene(seed=0):
+    from autoscoper_gb300 import scene as S
+    return S.make_scene(SHAPES, 0.4, (1024, 1024), 0.3, filters="chain", seed=seed,
+                        bone_offsets=[(0.0, 0.0, -45.0), (0.0, 0.0, 0.0), (0.0, 0.0, 45.0)], rot_range=10.0)
+
+
+def render_targets(sc):
+    """Radiographs = 1 - sum of the bones' DRRs at the ground truth (GPU)."""
+    from autoscoper_gb300 import api, geometry as G, scene as S
+    vols = [api.DeviceVolume(v) for v in sc.volumes]
+    for vi, v in enumerate(sc.views):
+        cam = v.camera
+        acc = np.zeros((cam.height, cam.width))
+        for b, dv in enumerate(vols):
+            xc = G.from_xyzypr(sc.truth[b])
+            mv = G.mul(G.inverse(cam.frame), xc)
+            imv = G.row_matrix(G.inverse(mv))
+            rp = sc.ray[vi][b]
+            acc += api.raycast(dv, imv, S.target_viewport(cam), rp.step, rp.intensity, rp.cutoff, cam.width,
+                               cam.height).to_host()
+        v.radiograph = S.radiograph_from_drr(acc, seed=vi)
+    rng = np.random.Generator(np.random.PCG64(99))
+    sc.poses = [S.perturb(t, rng, 5.0, 5.0) for t in sc.truth]
+    return vols
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 3 + i and r[3 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return ws, rank, local, pg
+
+
+def barrier(pg):
+    if pg:
+        pg.barrier()
+
+
+def allmax(pg, x):
+    if not pg:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(sc, n_evals, seed=5):
+    """Times the FP64 oracle's minimizationFunc on `n_evals` candidates."""
+    from oracle import oracle as O
+    tr = O.Tracker(sc)
+    rng = np.random.default_rng(seed)
+    t0 = time.perf_counter()
+    for k in range(n_evals):
+        b = k % len(sc.volumes)
+        tr.minimization_func(b, rng.uniform(-2, 2, 6))
+    dt = time.perf_counter() - t0
+    return n_evals / dt, dt
+
+
+def run_reference(args, ws, rank, pg):
+    if rank != 0:
+        return
+    sc = make_scene()
+    from autoscoper_gb300 import scene as S
+    # radiographs from the oracle itself (no GPU on this arm)
+    from oracle import oracle as O
+    tr = O.Tracker(sc)
+    for vi, v in enumerate(sc.views):
+        cam = v.camera
+        acc = np.zeros((cam.height, cam.width))
+        for b in range(len(sc.volumes)):
+            ok, m, _, _, _ = tr.view_setup(b, vi, sc.truth[b])
+            rp = sc.ray[vi][b]
+            acc += O.raycast(tr.vd[b], m, S.target_viewport(cam), rp.step, rp.intensity, rp.cutoff, cam.width,
+                             cam.height)
+        v.radiograph = S.radiograph_from_drr(acc, seed=vi)
+    per_step = 3
+    for _ in range(args.warmup):
+        cpu_sample(sc, 1)
+    times = []
+    for _ in range(args.steps):
+        _, dt = cpu_sample(sc, per_step)
+        times.append(dt)
+    v = per_step * args.steps / sum(times)
+    cores = os.cpu_count()
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "pose-evals/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": CONFIG,
+            "cpu_baseline": {"value": v, "unit": "pose-evals/s", "cores": cores, "kind": "port",
+                             "sample": f"{per_step} minimizationFunc evaluations per step on the full workload "
+                                       f"(FP64 oracle, OpenMP ray cast over {cores} threads)"},
+            "e2e": {"value": v, "unit": "pose-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
+    ap.add_argument("--iters", type=int, default=50)
+    args = ap.parse_args()
+    ws, rank, local, pg = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank, pg)
+        return
+    import ctypes as C
+    from autoscoper_gb300 import _lib as L
+    from autoscoper_gb300 import api
+    L.load()
+    L.call("asc_set_device", local)
+    sc = make_scene(seed=rank)
+    vols = render_targets(sc)
+    eng = api.Engine(sc, max_items=300, volumes=vols)
+    lib = L.load()
+    stream = C.c_void_p()
+    L.call("asc_stream_create", C.byref(stream))
+    ev0, ev1 = C.c_void_p(), C.c_void_p()
+    L.call("asc_event_create", C.byref(ev0))
+    L.call("asc_event_create", C.byref(ev1))
+    flush = api.DeviceArray((256 << 20,), np.uint8)  # 256 MB > 129 MB L2
+    nb, npart, iters = 3, 100, args.iters
+    best = np.zeros((nb, 6))
+    bcost = np.zeros(nb)
+    ev = C.c_longlong()
+
+    def step():
+        L.call("asc_engine_pso", eng.handle, npart, iters, 0.7298, 1.4962, 1.4962, -6.0, 6.0, 7,
+               best.ctypes.data_as(C.POINTER(C.c_double)), bcost.ctypes.data_as(C.POINTER(C.c_double)),
+               C.byref(ev), stream)
+
+    for _ in range(args.warmup):
+        step()
+    L.call("asc_stream_sync", stream)
+    # ---- device-resident throughput: K steps, L2 flushed between steps
+    ms_total = 0.0
+    with Clocks(local) as clk:
+        barrier(pg)
+        L.call("asc_device_sync")
+        for _ in range(args.steps):
+            L.call("asc_memset", flush.ptr, 1, flush.nbytes, stream)
+            L.call("asc_event_record", ev0, stream)
+            step()
+            L.call("asc_event_record", ev1, stream)
+            ms = C.c_float()
+            L.call("asc_event_elapsed", ev0, ev1, C.byref(ms))
+            ms_total += ms.value
+        L.call("asc_device_sync")
+        barrier(pg)
+    ms_step = allmax(pg, ms_total / args.steps)
+    evals_per_step = nb * npart * iters
+    value = ws * evals_per_step / (ms_step / 1000.0)
+    # ---- end to end through the public API: per step, the frame's two
+    # radiographs go host->device from pinned memory, the best poses come back
+    pinned = []
+    for v in sc.views:
+        p = C.c_void_p()
+        L.call("asc_host_alloc", C.byref(p), v.radiograph.nbytes)
+        C.memmove(p, v.radiograph.ctypes.data, v.radiograph.nbytes)
+        pinned.append(p)
+    h2d = sum(v.radiograph.nbytes for v in sc.views)
+    d2h = best.nbytes + bcost.nbytes
+    barrier(pg)
+    L.call("asc_device_sync")
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for vi, p in enumerate(pinned):
+            L.call("asc_image_update", eng.rads[vi].handle, p, stream)
+        step()  # returns after the D2H copy of best poses and costs
+    L.call("asc_device_sync")
+    e2e_s = allmax(pg, (time.perf_counter() - t0) / args.steps)
+    e2e = ws * evals_per_step / e2e_s
+    # ---- roofline of the dominant kernel (ray cast) on one PSO-iteration batch
+    L.call("asc_engine_profile", eng.handle, 1)
+    rng = np.random.default_rng(3)
+    bones = np.repeat(np.arange(nb), npart).astype(np.int32)
+    man = np.concatenate([rng.uniform(-5, 5, (nb * npart, 3)), rng.uniform(-5, 5, (nb * npart, 3))], 1)
+    phase = np.zeros(3)
+    reps = 5
+    samples = C.c_ulonglong()
+    pixels = C.c_ulonglong()
+    for r in range(reps + 1):
+        L.call("asc_memset", flush.ptr, 1, flush.nbytes, stream)
+        eng.eval(bones, man)
+        t3 = (C.c_float * 3)()
+        L.call("asc_engine_stats", eng.handle, t3, C.byref(samples), C.byref(pixels))
+        if r:
+            phase += np.array(t3[:])
+    phase /= reps
+    L.call("asc_engine_profile", eng.handle, 0)
+    ray_ms = phase[1]
+    alg_bytes = 16.0 * samples.value + 8.0 * pixels.value  # 8 taps x 2 B per sample + 4 taps x 2 B per pixel
+    achieved = alg_bytes / (ray_ms / 1000.0) / 1e9
+    peak, peak_kind = peaks()
+    traffic_path = os.path.join(ROOT, "profiles", "k_ray_traffic.json")
+    traffic = None
+    if os.path.exists(traffic_path):
+        t = json.load(open(traffic_path))
+        traffic = t.get("bytes_per_launch_scaled")
+    # ---- plain per-pose drop-in form on the same GPU (sampled)
+    nplain = 60
+    pb, pm = bones[::5][:nplain], man[::5][:nplain]
+    eng.eval(pb[:2], pm[:2], plain=True)
+    t0 = time.perf_counter()
+    eng.eval(pb, pm, plain=True)
+    plain_v = nplain / (time.perf_counter() - t0)
+    # ---- CPU baseline (oracle) on a bounded sample
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, dt = cpu_sample(sc, 3)
+        cpu = {"value": v, "unit": "pose-evals/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"3 minimizationFunc evaluations of this workload by the FP64 oracle ({dt:.1f} s)"}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "pose-evals/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32 (u16 volumes, FP64 pose/NCC combine)", "data": "synthetic",
+                "config": dict(CONFIG, l2="256 MB memset between timed steps", parallelism=f"replicas x{ws}"),
+                "e2e": {"value": e2e, "unit": "pose-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "gpu_launches": args.steps * (1 + 5 * iters),
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic,
+                             "kernel": "k_ray", "peak_kind": peak_kind,
+                             "note": "algorithmic gather bytes (16 B/sample + 8 B/pixel), served from L1/L2"},
+                "kernel_ms": {"setup": phase[0], "ray": phase[1], "view": phase[2]},
+                "work": {"samples_per_batch": samples.value, "pixels_per_batch": pixels.value, "batch": nb * npart},
+                "plain": {"value": plain_v, "unit": "pose-evals/s", "speedup": value / plain_v},
+                "cpu_baseline": cpu, "clocks": clk.summary(),
+                "best_cost": bcost.tolist()}
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,254 @@
+/*
+ * autoscoper_gb300.h -- C ABI of the GB300-native registration cost path.
+ *
+ * Drop-in boundary for Autoscoper's CUDA backend (namespace xromm::gpu in
+ * libautoscoper/src/gpu/cuda).  Every entry point returns an int status
+ * (ASC_OK = 0, negative on error) instead of exiting the process; none
+ * falls back to the CPU.  Image buffers are device float32 arrays, row-major
+ * with row stride = width, owned by the caller exactly as in the reference
+ * (Tracker.cpp:292-298).  `stream` is a cudaStream_t (NULL = legacy default
+ * stream); every call is asynchronous on it unless stated otherwise.
+ *
+ * Each declaration names the reference interface it replaces (paths are
+ * relative to the reference project root).  The C++ classes with the
+ * reference's own signatures are in autoscoper_gb300.hpp.
+ */
+#ifndef AUTOSCOPER_GB300_H
+#define AUTOSCOPER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ASC_OK 0
+#define ASC_ERR_ARG -1        /* bad argument (null pointer, size, kind) */
+#define ASC_ERR_CUDA -2       /* a CUDA runtime call failed */
+#define ASC_ERR_EMPTY -3      /* empty volume (reference: exit(0)) */
+#define ASC_ERR_RANGE -4      /* size beyond a buffer or a fixed limit */
+#define ASC_ERR_NOMEM -5      /* device allocation failed or over budget */
+#define ASC_ERR_TIMEOUT -6    /* a bounded device wait gave up */
+#define ASC_ERR_STATE -7      /* call out of order (e.g. no volume set) */
+
+/* Volume storage formats on the device (sampled in FP32 in every case). */
+#define ASC_STORE_U16 0   /* integer voxels as stored (u8/u16 input) */
+#define ASC_STORE_F16 1   /* voxels rounded to IEEE half */
+#define ASC_STORE_BF16 2  /* voxels rounded to bfloat16 */
+
+/* NCC/SAD coverage: the reference's sum() (Ncc_kernels.cu:151-187) folds
+ * each level's shared memory with s = T/2, T/4, ... and so drops partials
+ * whenever a level's thread count T is not a power of two.  ASC_SUM_TREE
+ * reproduces that coverage exactly; ASC_SUM_FULL sums every pixel. */
+#define ASC_SUM_TREE 0
+#define ASC_SUM_FULL 1
+
+typedef struct asc_volume_s *asc_volume;
+typedef struct asc_image_s *asc_image;
+typedef struct asc_engine_s *asc_engine;
+
+const char *asc_version(void);
+const char *asc_status_string(int status);
+/* Last CUDA error text seen by the library on this thread ("" if none). */
+const char *asc_last_error(void);
+
+/* ---- device memory helpers ----
+ * replaces gpu::cudaMallocWrap (libautoscoper/src/gpu/cuda/CudaWrap.cpp:59-62) */
+int asc_malloc(void **ptr, size_t bytes);
+int asc_free(void *ptr);
+int asc_memcpy_h2d(void *dst, const void *src, size_t bytes, void *stream);
+int asc_memcpy_d2h(void *dst, const void *src, size_t bytes, void *stream);
+int asc_memset(void *dst, int value, size_t bytes, void *stream);
+int asc_stream_sync(void *stream);
+int asc_device_sync(void);
+/* Plumbing for callers without their own CUDA runtime bindings (the ctypes
+ * layer, benchmarks): device selection, streams, events, pinned host memory. */
+int asc_set_device(int device);
+int asc_stream_create(void **stream);
+int asc_stream_destroy(void *stream);
+int asc_event_create(void **event);
+int asc_event_record(void *event, void *stream);
+int asc_event_elapsed(void *start, void *stop, float *ms);
+int asc_event_destroy(void *event);
+int asc_host_alloc(void **ptr, size_t bytes);
+int asc_host_free(void *ptr);
+
+/* ---- volumes ----
+ * replaces gpu::VolumeDescription::VolumeDescription(const Volume&)
+ * (libautoscoper/src/VolumeDescription.cpp:152-305): flips, crops to the
+ * non-zero box, records min/max and the normalisation constants, uploads.
+ * data: width*height*depth voxels (x fastest), bps 8 or 16; scale: voxel
+ * size in mm; flip: 0/1 per axis; storage: ASC_STORE_*. */
+int asc_volume_create(const void *data, int width, int height, int depth, int bps, const double scale[3],
+                      const int flip[3], int storage, asc_volume *out);
+/* invScale(), invTrans(), transCenter(), minValue(), maxValue() and the
+ * cropped dimensions (VolumeDescription.hpp:63-70). */
+int asc_volume_info(asc_volume vol, float inv_scale[3], float inv_trans[3], double trans_center[3],
+                    float *min_value, float *max_value, int dims[3]);
+int asc_volume_destroy(asc_volume vol);
+
+/* ---- DRR ray caster ----
+ * replaces RayCaster::setInvModelView + setViewport + render
+ * (libautoscoper/src/gpu/cuda/RayCaster.cpp:88-143) and volume_render
+ * (RayCaster_kernels.cu:81-104).  inv_model_view: the 16 doubles of
+ * CoordFrame::to_matrix_row_order of the camera->volume frame (the
+ * normalisation is folded in here, as setInvModelView does);
+ * viewport: (x, y, width, height) on the film plane; visible = 0 clears. */
+int asc_raycast(asc_volume vol, const double inv_model_view[16], const float viewport[4], float sample_distance,
+                float ray_intensity, float cutoff, int visible, float *out, int width, int height, void *stream);
+
+/* ---- radiograph and background samplers ----
+ * replaces RadRenderer::set_rad (RadRenderer.cpp:81-105) and
+ * BackgroundRenderer::set_back (BackgroundRenderer.cpp:74-86): an image held
+ * on the device.  bps: 8 or 16 (radiograph, normalized) or 32 (float32
+ * background, read as stored). */
+int asc_image_create(const void *data, int width, int height, int bps, asc_image *out);
+/* Replaces the pixels of an image of the same size (the per-frame
+ * Video::set_frame + set_rad of Tracker::optimize, Tracker.cpp:381-386)
+ * without reallocating; asynchronous on `stream`. */
+int asc_image_update(asc_image img, const void *data, void *stream);
+int asc_image_destroy(asc_image img);
+/* RadRenderer::render (RadRenderer.cpp:123-142, image_render_kernel
+ * RadRenderer_kernels.cu:85-116): out = 1 - bilinear(rad) inside the
+ * image plane, 0 outside.  image_plane = the camera viewport. */
+int asc_rad_render(asc_image img, const float image_plane[4], const float viewport[4], float *out, int width,
+                   int height, void *stream);
+/* BackgroundRenderer::render (BackgroundRenderer.cpp:88-124): out =
+ * (threshold <= bilinear(bg)) ? 1 : 0 inside, 0 outside. */
+int asc_background_render(asc_image img, const float image_plane[4], const float viewport[4], float threshold,
+                          float *out, int width, int height, void *stream);
+
+/* ---- elementwise ----
+ * drr_background (DRRBackground_kernels.cu:47-75), multiply
+ * (Mult_kernels.cu:49-77), merge (Merger_kernels.cu:49-75), composite
+ * (Compositor_kernels.cu:53-88; writes 3*w*h interleaved RGB), fill
+ * (Compositor_kernels.cu:64-68; this one honours `value`, the reference
+ * always writes 1.0). */
+int asc_drr_background(const float *src, float *dst, int width, int height, void *stream);
+int asc_multiply(const float *a, const float *b, float *dst, int width, int height, void *stream);
+int asc_merge(const float *a, const float *b, float *dst, int width, int height, void *stream);
+int asc_composite(const float *a, const float *b, const float *c, const float *d, float *dst, int width, int height,
+                  void *stream);
+int asc_fill(float *dst, size_t count, float value, void *stream);
+
+/* ---- filters ----
+ * SobelFilter::apply (SobelFilter_kernels.cu:63-113), ContrastFilter::apply
+ * (ContrastFilter_kernels.cu:62-96), GaussianFilter::apply
+ * (GaussianFilter.cpp:73-134, GaussianFilter_kernels.cu:61-97),
+ * SharpenFilter::apply (SharpenFilter.cpp:58-158, SharpenFilter_kernels.cu:74-129).
+ * in and out must not alias.  A Gaussian/Sharpen radius with
+ * 2*floor(3r)+1 == 1 copies the image. */
+int asc_sobel(const float *in, float *out, int width, int height, float scale, float blend, void *stream);
+int asc_contrast(const float *in, float *out, int width, int height, float alpha, float beta, int size,
+                 void *stream);
+int asc_gaussian(const float *in, float *out, int width, int height, float radius, void *stream);
+int asc_sharpen(const float *in, float *out, int width, int height, float radius, float contrast, float threshold,
+                void *stream);
+
+/* ---- cost reductions ----
+ * replaces gpu::ncc_init / ncc (Ncc_kernels.cu:87-134) and gpu::hdist_init /
+ * hdist (HDist_kernels.cu:50-134).  asc_ncc_init(max_n) sizes the per-block
+ * partial buffer used by asc_ncc/asc_hdist (max_n = 0 frees it).  The result
+ * is written to *result_dev (a device double) without a host sync; NCC
+ * keeps the reference's 1e5 value for a denominator below 1e-5.
+ * `coverage` is ASC_SUM_TREE or ASC_SUM_FULL. */
+int asc_ncc_init(unsigned max_n);
+int asc_ncc(const float *f, const float *g, const float *mask, unsigned n, int coverage, double *result_dev,
+            void *stream);
+int asc_hdist(const float *f, const float *g, const float *mask, unsigned n, int coverage, double *result_dev,
+              void *stream);
+/* Blocking convenience forms returning the value on the host (the
+ * reference's float ncc(...) / hdist(...) signatures). */
+int asc_ncc_host(const float *f, const float *g, const float *mask, unsigned n, int coverage, double *result,
+                 void *stream);
+int asc_hdist_host(const float *f, const float *g, const float *mask, unsigned n, int coverage, double *result,
+                   void *stream);
+
+/* ---- batched registration engine (Tracker::minimizationFunc batched) ----
+ * An engine holds a scene resident on the device: cameras, volumes,
+ * radiographs, filter chains, ray-caster settings, pivots and base poses.
+ * asc_engine_eval scores many (bone, manipulator) candidates in one pass of
+ * fused launches; see asc_engine.h-level docs in autoscoper_gb300.hpp. */
+typedef struct {
+  int kind;          /* 0 contrast, 1 sobel, 3 gaussian, 4 sharpen (Filter.hpp:59-66) */
+  int enabled;
+  float p0, p1, p2;  /* sobel: scale, blend; contrast: alpha, beta, size;
+                        gaussian: radius; sharpen: radius, contrast, threshold */
+} asc_filter_desc;
+
+typedef struct {
+  double frame[12];       /* camera -> world CoordFrame (rotation columns, translation) */
+  double viewport[4];     /* Camera::viewport() */
+  double image_plane[12]; /* Camera::image_plane() */
+  asc_image radiograph;   /* current frame's radiograph */
+  asc_image background;   /* optional float image (NULL = none) */
+  float bg_threshold;     /* < 0 disables the background mask (View.cpp:171-194) */
+  int n_drr_filters, n_rad_filters;
+  asc_filter_desc drr_filters[8];
+  asc_filter_desc rad_filters[8];
+} asc_view_desc;
+
+typedef struct {
+  asc_volume volume;
+  double pivot[12];       /* volume matrix (Trial::getVolumeMatrix after the pivot translate) */
+  double base_pose[6];    /* current pose xyzypr (the values the reference reads from its curves) */
+  float step[4], intensity[4], cutoff[4];  /* RayCaster settings per view */
+} asc_bone_desc;
+
+int asc_engine_create(int n_views, const asc_view_desc *views, int n_bones, const asc_bone_desc *bones,
+                      int render_width, int render_height, int max_items, int coverage, int cf_model,
+                      asc_engine *out);
+int asc_engine_destroy(asc_engine e);
+int asc_engine_set_base_pose(asc_engine e, int bone, const double xyzypr[6]);
+int asc_engine_set_radiograph(asc_engine e, int view, asc_image radiograph);
+/* Scores n candidates: bone[i] and manip[6*i] (xyz mm + axis-angle degrees,
+ * CoordFrame::from_xyzAxis_angle).  cost_dev (device, n doubles) receives
+ * minimizationFunc's value; view_cost_dev (optional, n*n_views) the per-view
+ * terms of trackFrame.  Inputs are device pointers. */
+int asc_engine_eval(asc_engine e, int n, const int *bone_dev, const double *manip_dev, double *cost_dev,
+                    double *view_cost_dev, void *stream);
+/* Host-pointer form: copies the candidates in and the costs out (blocking). */
+int asc_engine_eval_host(asc_engine e, int n, const int *bone, const double *manip, double *cost,
+                         double *view_cost, void *stream);
+/* The plain per-pose drop-in form of the same evaluation: for each candidate,
+ * Tracker::trackFrame's call sequence (Tracker.cpp:603-770) over the plain
+ * per-operator kernels above, with the NCC read back to the host after every
+ * view as the reference does.  Host pointers; blocking. */
+int asc_engine_eval_plain(asc_engine e, int n, const int *bone, const double *manip, double *cost,
+                          double *view_cost, void *stream);
+/* Device pointers of the last evaluation's DRR images and per-item-view
+ * layout, for inspection/tests: layout[5*k] = (ok, width, height, offset, tiles). */
+int asc_engine_debug(asc_engine e, const float **drr_dev, const int **layout_dev);
+/* Instrumentation of asc_engine_eval: with profiling on, events bracket the
+ * set-up, ray-cast and view kernels of each evaluation; stats returns the
+ * last evaluation's phase times (ms) and its trilinear sample and pixel
+ * counts (the work figures of the roofline). */
+int asc_engine_profile(asc_engine e, int enable);
+int asc_engine_stats(asc_engine e, float ms[3], unsigned long long *samples, unsigned long long *pixels);
+
+/* ---- device-resident optimizers ----
+ * Synchronous batched PSO over all bones at once: n_particles per bone,
+ * n_iter iterations; inertia w, c1, c2; particles start uniform in
+ * [lo, hi]^6 (particle 0 at the zero manipulator, PSO.cpp:207-214).  Each
+ * iteration (velocity/position update, scoring, best updates) is one CUDA
+ * graph launch.  best_manip (host, 6 per bone) and best_cost (host, per
+ * bone) receive gBest.  evals_out (optional) the number of poses scored. */
+int asc_engine_pso(asc_engine e, int n_particles, int n_iter, double w, double c1, double c2, double lo, double hi,
+                   uint64_t seed, double *best_manip, double *best_cost, long long *evals_out, void *stream);
+
+/* Reference-sequential PSO on the host (PSO.cpp:198-295, asynchronous gBest,
+ * glibc rand() after srand(seed), omega 0.8 * 0.9^epoch, c1 = c2 = 1.5),
+ * with a caller-supplied cost.  Used to reproduce reference trajectories. */
+typedef double (*asc_cost_fn)(const double *x, void *ctx);
+int asc_pso_sequential(asc_cost_fn cost, void *ctx, int n_particles, float lo, float hi, unsigned max_epochs,
+                       unsigned max_stall, unsigned seed, float best_pos[6], float *best_cost);
+/* AMOEBA (DownhillSimplex.cpp:39-172) with a caller-supplied cost:
+ * p = (ndim+1) x ndim vertices row-major, y = their values (in/out). */
+int asc_amoeba(asc_cost_fn cost, void *ctx, double *p, double *y, int ndim, double ftol, int *iterations);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
