@@ -38,6 +38,7 @@ class BoneDesc(C.Structure):
 
 # name: (restype, argtypes)
 SIGNATURES = {
+    "asc_set_option": (i32, [i32, i32]),
     "asc_version": (C.c_char_p, []),
     "asc_status_string": (C.c_char_p, [i32]),
     "asc_last_error": (C.c_char_p, []),

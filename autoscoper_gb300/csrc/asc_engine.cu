@@ -62,6 +62,7 @@ struct BoneDev {
   float inv_scale[3], inv_trans[3];
   double pivot[12], pivot_inv[12], base[6];
   float step[MAX_VIEWS], scale[MAX_VIEWS], cutoff_raw[MAX_VIEWS];
+  const uint8_t* occ[MAX_VIEWS];  // empty-cell grids per view's cutoff
 };
 
 struct SceneDev {
@@ -238,12 +239,12 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
 
 // ---------------------------------------------------------------- k_ray
 template <int STORE>
-__device__ __forceinline__ float march_any(const DevVolume& V, const RaySetup& r, float cut)
+__device__ __forceinline__ float march_any(const DevVolume& V, const uint8_t* occ, const RaySetup& r, float cut)
 {
-  return march<STORE>(V, r.X0, r.dX, r.Y0, r.dY, r.Z0, r.dZ, r.tnear, r.tfar, cut);
+  return march<STORE>(V, occ, r.X0, r.dX, r.Y0, r.dY, r.Z0, r.dZ, r.tnear, r.tfar, cut);
 }
 
-__global__ void __launch_bounds__(256) k_ray(const SceneDev* __restrict__ sc, Bufs b)
+__global__ void __launch_bounds__(256) k_ray(const SceneDev* __restrict__ sc, Bufs b, int skip)
 {
   __shared__ int s_tile;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -274,13 +275,14 @@ __global__ void __launch_bounds__(256) k_ray(const SceneDev* __restrict__ sc, Bu
     }
     if (hit) {
       float cut = B.cutoff_raw[v];
+      const uint8_t* occ = skip ? B.occ[v] : nullptr;
       float acc;
       if (B.vol.storage == ASC_STORE_BF16)
-        acc = march_any<ASC_STORE_BF16>(B.vol, rs, cut);
+        acc = march_any<ASC_STORE_BF16>(B.vol, occ, rs, cut);
       else if (B.vol.storage == ASC_STORE_F16)
-        acc = march_any<ASC_STORE_F16>(B.vol, rs, cut);
+        acc = march_any<ASC_STORE_F16>(B.vol, occ, rs, cut);
       else
-        acc = march_any<ASC_STORE_U16>(B.vol, rs, cut);
+        acc = march_any<ASC_STORE_U16>(B.vol, occ, rs, cut);
       d = acc * B.scale[v];
     }
     b.drr[r.pix + (long long)y * r.w + x] = fminf(fmaxf(d, 0.f), 1.f);
@@ -302,96 +304,96 @@ __device__ __forceinline__ bool inside(const Region& g, int ry, int rx)
 
 // Applies one filter from `in` to `out` over the square band
 // [lo, hi) x [lo, hi) of region coordinates; positions outside the image get
-// 0.  `tmp` holds the horizontal pass of a Gaussian/Sharpen blur.
-__device__ void apply_stage(const FilterDev& f, const float* in, float* out, float* tmp, const Region& g, int lo,
-                            int hi)
+// 0.  `tmp` holds the horizontal pass of a Gaussian/Sharpen blur, `wsh` its
+// 1-D weights.  Threads map to (row, column) as 8 x 32.
+__device__ void apply_stage(const FilterDev& f, const float* in, float* out, float* tmp, float* wsh, const Region& g,
+                            int lo, int hi)
 {
-  const int E = g.E, n = hi - lo;
-  if (f.kind == 3 || f.kind == 4) {
-    const int R = f.R;
-    // horizontal pass over rows [lo - R, hi + R)
-    const int rows = n + 2 * R;
-    for (int i = threadIdx.x; i < rows * n; i += blockDim.x) {
-      int ry = lo - R + i / n, rx = lo + i % n;
-      const float* p = in + ry * E + rx - R;
-      float s = 0.f;
-      for (int k = 0; k < f.K; ++k) s = fmaf(f.g[k], p[k], s);
-      tmp[ry * E + rx] = s;
-    }
+  const int E = g.E;
+  const int ty = threadIdx.x >> 5, tx = threadIdx.x & 31;
+  const int kind = f.kind, K = f.K, R = f.R;
+  const float p0 = f.p0, p1 = f.p1, p2 = f.p2;
+  if (kind == 3 || kind == 4) {
+    if (threadIdx.x < K) wsh[threadIdx.x] = f.g[threadIdx.x];
     __syncthreads();
-    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
-      int ry = lo + i / n, rx = lo + i % n;
-      float r = 0.f;
-      if (inside(g, ry, rx)) {
-        float blur = 0.f;
-        for (int k = 0; k < f.K; ++k) blur = fmaf(f.g[k], tmp[(ry - R + k) * E + rx], blur);
-        if (f.kind == 3) {
-          r = fminf(fmaxf(blur, 0.f), 1.f);
-        } else {
-          float v = in[ry * E + rx];
-          r = fabsf(v - blur) > f.p2 ? fminf(fmaxf(v + f.p1 * (v - blur), 0.f), 1.f) : v;
-        }
+    // horizontal pass over rows [lo - R, hi + R)
+    for (int ry = lo - R + ty; ry < hi + R; ry += 8)
+      for (int rx = lo + tx; rx < hi; rx += 32) {
+        const float* p = in + ry * E + rx - R;
+        float s = 0.f;
+        for (int k = 0; k < K; ++k) s = fmaf(wsh[k], p[k], s);
+        tmp[ry * E + rx] = s;
       }
-      out[ry * E + rx] = r;
-    }
-  } else if (f.kind == 1) {
-    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
-      int ry = lo + i / n, rx = lo + i % n;
-      float r = 0.f;
-      if (inside(g, ry, rx)) {
-        int x = g.x0 + rx, y = g.y0 + ry;
-        int xm = x > 0 ? -1 : 0, xp = x < g.w - 1 ? 1 : 0, ym = y > 0 ? -1 : 0, yp = y < g.h - 1 ? 1 : 0;
-        const float* c = in + ry * E + rx;
-        float p00 = c[ym * E + xm], p01 = c[ym * E], p02 = c[ym * E + xp];
-        float p10 = c[xm], p11 = c[0], p12 = c[xp];
-        float p20 = c[yp * E + xm], p21 = c[yp * E], p22 = c[yp * E + xp];
-        float horz = p02 + 2 * p12 + p22 - p00 - 2 * p10 - p20;
-        float vert = p00 + 2 * p01 + p02 - p20 - 2 * p21 - p22;
-        float grad = sqrtf(horz * horz + vert * vert);
-        float s = f.p1 < 0.5f ? f.p0 * grad + 2.0f * f.p1 * p11 : 2.0f * (1.0f - f.p1) * f.p0 * grad + p11;
-        r = fminf(fmaxf(s, 0.f), 1.f);
-      }
-      out[ry * E + rx] = r;
-    }
-  } else if (f.kind == 0) {
-    const int size = f.K;
-    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
-      int ry = lo + i / n, rx = lo + i % n;
-      float r = 0.f;
-      if (inside(g, ry, rx)) {
-        int x = g.x0 + rx, y = g.y0 + ry;
-        int i0 = max(y - size / 2, 0), i1 = min(y + (size + 1) / 2, g.h);
-        int j0 = max(x - size / 2, 0), j1 = min(x + (size + 1) / 2, g.w);
-        float cnt = 0.f, s = 0.f;
-        for (int yy = i0; yy < i1; ++yy)
-          for (int xx = j0; xx < j1; ++xx) {
-            cnt += 1.0f;
-            s += in[(yy - g.y0) * E + (xx - g.x0)];
+    __syncthreads();
+    for (int ry = lo + ty; ry < hi; ry += 8)
+      for (int rx = lo + tx; rx < hi; rx += 32) {
+        float r = 0.f;
+        if (inside(g, ry, rx)) {
+          const float* p = tmp + (ry - R) * E + rx;
+          float blur = 0.f;
+          for (int k = 0; k < K; ++k) blur = fmaf(wsh[k], p[k * E], blur);
+          if (kind == 3) {
+            r = fminf(fmaxf(blur, 0.f), 1.f);
+          } else {
+            float v = in[ry * E + rx];
+            r = fabsf(v - blur) > p2 ? fminf(fmaxf(v + p1 * (v - blur), 0.f), 1.f) : v;
           }
-        float axy = s / cnt, v = in[ry * E + rx];
-        r = axy > 0.01f ? powf(axy, f.p0 - f.p1) * powf(v, f.p1) : 0.0f;
+        }
+        out[ry * E + rx] = r;
       }
-      out[ry * E + rx] = r;
-    }
-  } else {
-    for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
-      int ry = lo + i / n, rx = lo + i % n;
-      out[ry * E + rx] = in[ry * E + rx];
-    }
+  } else if (kind == 1) {
+    for (int ry = lo + ty; ry < hi; ry += 8)
+      for (int rx = lo + tx; rx < hi; rx += 32) {
+        float r = 0.f;
+        if (inside(g, ry, rx)) {
+          int x = g.x0 + rx, y = g.y0 + ry;
+          int xm = x > 0 ? -1 : 0, xp = x < g.w - 1 ? 1 : 0, ym = y > 0 ? -E : 0, yp = y < g.h - 1 ? E : 0;
+          const float* c = in + ry * E + rx;
+          float p00 = c[ym + xm], p01 = c[ym], p02 = c[ym + xp];
+          float p10 = c[xm], p11 = c[0], p12 = c[xp];
+          float p20 = c[yp + xm], p21 = c[yp], p22 = c[yp + xp];
+          float horz = p02 + 2 * p12 + p22 - p00 - 2 * p10 - p20;
+          float vert = p00 + 2 * p01 + p02 - p20 - 2 * p21 - p22;
+          float grad = sqrtf(horz * horz + vert * vert);
+          float s = p1 < 0.5f ? p0 * grad + 2.0f * p1 * p11 : 2.0f * (1.0f - p1) * p0 * grad + p11;
+          r = fminf(fmaxf(s, 0.f), 1.f);
+        }
+        out[ry * E + rx] = r;
+      }
+  } else if (kind == 0) {
+    const int size = K;
+    for (int ry = lo + ty; ry < hi; ry += 8)
+      for (int rx = lo + tx; rx < hi; rx += 32) {
+        float r = 0.f;
+        if (inside(g, ry, rx)) {
+          int x = g.x0 + rx, y = g.y0 + ry;
+          int i0 = max(y - size / 2, 0), i1 = min(y + (size + 1) / 2, g.h);
+          int j0 = max(x - size / 2, 0), j1 = min(x + (size + 1) / 2, g.w);
+          float cnt = 0.f, s = 0.f;
+          for (int yy = i0; yy < i1; ++yy)
+            for (int xx = j0; xx < j1; ++xx) {
+              cnt += 1.0f;
+              s += in[(yy - g.y0) * E + (xx - g.x0)];
+            }
+          float axy = s / cnt, v = in[ry * E + rx];
+          r = axy > 0.01f ? powf(axy, p0 - p1) * powf(v, p1) : 0.0f;
+        }
+        out[ry * E + rx] = r;
+      }
   }
   __syncthreads();
 }
 
 // Runs a filter chain on buf[0] (valid on [eh - H, eh + VT + H)); returns the
 // buffer index holding the result on the tile band [eh, eh + VT).
-__device__ int run_chain(const FilterDev* fl, int nf, int H, float* bufs[3], const Region& g, int eh)
+__device__ int run_chain(const FilterDev* fl, int nf, int H, float* bufs[3], float* wsh, const Region& g, int eh)
 {
   int cur = 0, halo = H;
   for (int s = 0; s < nf; ++s) {
     const FilterDev& f = fl[s];
     int nh = halo - f.R;
     int nxt = cur == 0 ? 1 : 0;
-    apply_stage(f, bufs[cur], bufs[nxt], bufs[2], g, eh - nh, eh + VT + nh);
+    apply_stage(f, bufs[cur], bufs[nxt], bufs[2], wsh, g, eh - nh, eh + VT + nh);
     cur = nxt;
     halo = nh;
   }
@@ -423,13 +425,15 @@ __device__ void bsum(float (&v)[N], float* red)
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(256) k_view(const SceneDev* __restrict__ sc, Bufs b, double* __restrict__ cost,
+__global__ void __launch_bounds__(256, 3) k_view(const SceneDev* __restrict__ sc, Bufs b, double* __restrict__ cost,
                                               double* __restrict__ view_cost_out)
 {
   extern __shared__ float smem[];
   __shared__ int s_tile;
   __shared__ bool s_last;
   __shared__ float red[8 * 6];
+  __shared__ float wsh[32];
+  const int ty = threadIdx.x >> 5, tx = threadIdx.x & 31;
   const int E = sc->E, eh = (E - VT) / 2;
   float* bufs[3] = {smem, smem + E * E, smem + 2 * E * E};
   float* fdrr = smem + 3 * E * E;        // VT x VT final DRR
@@ -451,13 +455,12 @@ __global__ void __launch_bounds__(256) k_view(const SceneDev* __restrict__ sc, B
     const float* drr = b.drr + r.pix;
     // ---- DRR chain
     {
-      const int lo = eh - V.h_drr, n = VT + 2 * V.h_drr;
-      for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
-        int ry = lo + i / n, rx = lo + i % n;
-        bufs[0][ry * E + rx] = inside(g, ry, rx) ? __ldg(drr + (long long)(g.y0 + ry) * r.w + g.x0 + rx) : 0.f;
-      }
+      const int lo = eh - V.h_drr, hi = eh + VT + V.h_drr;
+      for (int ry = lo + ty; ry < hi; ry += 8)
+        for (int rx = lo + tx; rx < hi; rx += 32)
+          bufs[0][ry * E + rx] = inside(g, ry, rx) ? __ldg(drr + (long long)(g.y0 + ry) * r.w + g.x0 + rx) : 0.f;
       __syncthreads();
-      int res = run_chain(V.fdrr, V.n_drr, V.h_drr, bufs, g, eh);
+      int res = run_chain(V.fdrr, V.n_drr, V.h_drr, bufs, wsh, g, eh);
       for (int i = threadIdx.x; i < VT * VT; i += blockDim.x)
         fdrr[i] = bufs[res][(eh + i / VT) * E + eh + i % VT];
       __syncthreads();
@@ -465,16 +468,16 @@ __global__ void __launch_bounds__(256) k_view(const SceneDev* __restrict__ sc, B
     // ---- radiograph crop and its chain
     int rres;
     {
-      const int lo = eh - V.h_rad, n = VT + 2 * V.h_rad;
-      for (int i = threadIdx.x; i < n * n; i += blockDim.x) {
-        int ry = lo + i / n, rx = lo + i % n;
-        float val = 0.f, s, tt;
-        if (inside(g, ry, rx) && image_coords(V.ipf, r.vp, g.x0 + rx, g.y0 + ry, r.w, r.h, s, tt))
-          val = 1.0f - bilinear(V.rad, V.rad_bps, V.rad_w, V.rad_h, s, tt);
-        bufs[0][ry * E + rx] = val;
-      }
+      const int lo = eh - V.h_rad, hi = eh + VT + V.h_rad;
+      for (int ry = lo + ty; ry < hi; ry += 8)
+        for (int rx = lo + tx; rx < hi; rx += 32) {
+          float val = 0.f, s, tt;
+          if (inside(g, ry, rx) && image_coords(V.ipf, r.vp, g.x0 + rx, g.y0 + ry, r.w, r.h, s, tt))
+            val = 1.0f - bilinear(V.rad, V.rad_bps, V.rad_w, V.rad_h, s, tt);
+          bufs[0][ry * E + rx] = val;
+        }
       __syncthreads();
-      rres = run_chain(V.frad, V.n_rad, V.h_rad, bufs, g, eh);
+      rres = run_chain(V.frad, V.n_rad, V.h_rad, bufs, wsh, g, eh);
     }
     // ---- masks and moments (Tracker.cpp:744-770)
     const unsigned n = (unsigned)r.w * (unsigned)r.h;
@@ -818,6 +821,13 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
       B.step[v] = bones[i].step[v];
       B.scale[v] = bones[i].step[v] * vh->dev.norm / bones[i].intensity[v];
       B.cutoff_raw[v] = bones[i].cutoff[v] / vh->dev.norm;
+      uint8_t* occ = nullptr;
+      if (e->alloc(occ, occupancy_cells(vh->dev))) {
+        delete e;
+        return ASC_ERR_NOMEM;
+      }
+      build_occupancy(vh->dev, B.cutoff_raw[v], occ, nullptr);
+      B.occ[v] = occ;
     }
   }
   e->max_items = max_items;
@@ -908,7 +918,7 @@ static int engine_launch(asc_engine e, int n, const int* bone, const double* man
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[0], s));
   k_setup<<<1, 1024, 0, s>>>(e->dev, n, bone, manip, e->b, cost, vcost);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[1], s));
-  k_ray<<<e->sms * 8, 256, 0, s>>>(e->dev, e->b);
+  k_ray<<<e->sms * 8, 256, 0, s>>>(e->dev, e->b, g_empty_skip);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[2], s));
   k_view<<<e->sms * 4, 256, e->smem, s>>>(e->dev, e->b, cost, vcost);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[3], s));
@@ -1093,7 +1103,8 @@ ASC_API int asc_engine_eval_plain(asc_engine e, int n, const int* bone, const do
           vc = 1.0 - 1e5;
         } else {
           float vpf[4] = {(float)vp[0], (float)vp[1], (float)vp[2], (float)vp[3]};
-          int rc = raycast_launch(B.vol, m, vpf, BD.step[v], BD.intensity[v], BD.cutoff[v], e->p_drr, w, h, s);
+          int rc = raycast_launch(B.vol, g_empty_skip ? B.occ[v] : nullptr, m, vpf, BD.step[v], BD.intensity[v],
+                                  BD.cutoff[v], e->p_drr, w, h, s);
           float *d = e->p_drr, *o = e->p_tmp;
           if (!rc) rc = chain_plain(VD.drr_filters, VD.n_drr_filters, d, o, w, h, s);
           // the DRR chain ping-pongs p_drr/p_tmp and leaves one of them free (o);

@@ -45,6 +45,8 @@ struct DevVolume {
 struct asc_volume_host {
   DevVolume dev;
   uint32_t* pairs;
+  uint8_t* occ;     // occupancy grid of the plain ray caster ...
+  float occ_cutoff; // ... for this raw cutoff (NaN = not built)
   float inv_scale[3], inv_trans[3];
   double trans_center[3];
   float min_value, max_value;
@@ -84,24 +86,56 @@ __device__ __forceinline__ void tap(float X, int& k, float& a)
   a = __fadd_rn(X, -__fadd_rn(t, -M));
 }
 
+// Occupancy of 8x8x8-voxel cells for one cutoff: cell (cx, cy, cz) is 0 when
+// every voxel of [8c-1, 8c+9) on each axis (the taps of any sample whose
+// lower tap lies in the cell) is <= cutoff.  A trilinear sample is a convex
+// combination of its taps, so such a sample is <= cutoff and adds exactly
+// nothing to the DRR (RayCaster_kernels.cu:189); the march skips it.
+constexpr int OCC = 8;
+
 // One ray of cuda_volume_render_kernel (RayCaster_kernels.cu:144-195) from
 // t = far down to t > near in unit steps, sampling at voxel coordinates
-// (X0 + t dX, Y0 + t dY, Z0 + t dZ).  Returns the sum of raw samples above
-// cutoff_raw (the caller scales by step * norm / intensity).
+// (X0 + t dX, Y0 + t dY, Z0 + t dZ).  Returns the compensated (Kahan) sum of
+// raw samples above cutoff_raw (the caller scales by step * norm /
+// intensity).  With `occ`, runs of samples inside empty cells are stepped
+// over without being read: the same samples contribute, in the same order.
 template <int STORE>
-__device__ __forceinline__ float march(const DevVolume& V, float X0, float dX, float Y0, float dY, float Z0, float dZ,
-                                       float tnear, float tfar, float cutoff_raw)
+__device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __restrict__ occ, float X0, float dX,
+                                       float Y0, float dY, float Z0, float dZ, float tnear, float tfar,
+                                       float cutoff_raw)
 {
   const uint32_t* __restrict__ P = V.pairs;
   const int nx = V.nx, ny = V.ny, nz = V.nz;
   const int sxy = nx * ny;
-  float acc = 0.f;
-  for (float t = tfar; t > tnear; t -= 1.0f) {
+  const int bx = (nx + OCC - 1) / OCC, by = (ny + OCC - 1) / OCC, bz = (nz + OCC - 1) / OCC;
+  float acc = 0.f, comp = 0.f;
+  float t = tfar;
+  while (t > tnear) {
+    const float X = fmaf(t, dX, X0), Y = fmaf(t, dY, Y0), Z = fmaf(t, dZ, Z0);
+    if (occ) {
+      const int cx = min(max(__float2int_rd((X - 0.5f) * (1.0f / OCC)), 0), bx - 1);
+      const int cy = min(max(__float2int_rd((Y - 0.5f) * (1.0f / OCC)), 0), by - 1);
+      const int cz = min(max(__float2int_rd((Z - 0.5f) * (1.0f / OCC)), 0), bz - 1);
+      if (!__ldg(occ + (cz * by + cy) * bx + cx)) {
+        // whole steps until the lower tap leaves the cell; t decreases, so a
+        // coordinate moves by -d per step
+        float s = 3.0e38f;
+        if (dX > 0.f) s = fminf(s, (X - (OCC * cx + 0.5f)) / dX);
+        if (dX < 0.f) s = fminf(s, ((OCC * cx + OCC + 0.5f) - X) / -dX);
+        if (dY > 0.f) s = fminf(s, (Y - (OCC * cy + 0.5f)) / dY);
+        if (dY < 0.f) s = fminf(s, ((OCC * cy + OCC + 0.5f) - Y) / -dY);
+        if (dZ > 0.f) s = fminf(s, (Z - (OCC * cz + 0.5f)) / dZ);
+        if (dZ < 0.f) s = fminf(s, ((OCC * cz + OCC + 0.5f) - Z) / -dZ);
+        const float m = fminf(fmaxf(floorf(s - 0.01f), 0.f), 1.0e6f);
+        t -= m + 1.0f;
+        continue;
+      }
+    }
     int ix, iy, iz;
     float ax, ay, az;
-    tap(fmaf(t, dX, X0), ix, ax);
-    tap(fmaf(t, dY, Y0), iy, ay);
-    tap(fmaf(t, dZ, Z0), iz, az);
+    tap(X, ix, ax);
+    tap(Y, iy, ay);
+    tap(Z, iz, az);
     // clamp-to-edge; below the first texel both taps are texel 0
     if (ix < 0) { ix = 0; ax = 0.f; }
     ix = min(ix, nx - 1);
@@ -128,10 +162,26 @@ __device__ __forceinline__ float march(const DevVolume& V, float X0, float dX, f
     float f0 = fmaf(ay, e10 - e00, e00);
     float f1 = fmaf(ay, e11 - e01, e01);
     float s = fmaf(az, f1 - f0, f0);
-    acc += s > cutoff_raw ? s : 0.f;
+    if (s > cutoff_raw) {  // a sample at or below the cutoff leaves the sum untouched
+      const float y = s - comp;
+      const float tt = acc + y;
+      comp = (tt - acc) - y;
+      acc = tt;
+    }
+    t -= 1.0f;
   }
   return acc;
 }
+
+// Builds the occupancy grid of a device volume for one raw cutoff.
+void build_occupancy(const DevVolume& V, float cutoff_raw, uint8_t* occ, cudaStream_t s);
+inline size_t occupancy_cells(const DevVolume& V)
+{
+  return (size_t)((V.nx + OCC - 1) / OCC) * ((V.ny + OCC - 1) / OCC) * ((V.nz + OCC - 1) / OCC);
+}
+
+// Global switches (asc_set_option).
+extern int g_empty_skip;
 
 // Per-ray set-up of cuda_volume_render_kernel: pixel (x, y) of a w x h image
 // over `vp`, camera->volume matrix m (3x4 row-major, normalisation folded).
@@ -424,7 +474,7 @@ int gauss_1d(float radius, float* g, int cap);
 int launch_filter(const asc_filter_desc& f, const float* in, float* out, int w, int h, cudaStream_t s);
 
 // One plain ray-cast launch with an already folded float matrix.
-int raycast_launch(const DevVolume& V, const float* m12, const float* vp, float step, float intensity, float cutoff,
-                   float* out, int w, int h, cudaStream_t s);
+int raycast_launch(const DevVolume& V, const uint8_t* occ, const float* m12, const float* vp, float step,
+                   float intensity, float cutoff, float* out, int w, int h, cudaStream_t s);
 
 }  // namespace asc

@@ -56,7 +56,8 @@ struct RayArgs {
 };
 
 template <int STORE>
-__global__ void __launch_bounds__(256) k_raycast(DevVolume V, RayArgs a, float* __restrict__ out, int w, int h)
+__global__ void __launch_bounds__(256) k_raycast(DevVolume V, const uint8_t* __restrict__ occ, RayArgs a,
+                                                 float* __restrict__ out, int w, int h)
 {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
@@ -65,7 +66,7 @@ __global__ void __launch_bounds__(256) k_raycast(DevVolume V, RayArgs a, float* 
   RaySetup r;
   float d = 0.f;
   if (ray_setup(a.m, a.vp, x, y, w, h, a.step, V.nx, V.ny, V.nz, r))
-    d = march<STORE>(V, r.X0, r.dX, r.Y0, r.dY, r.Z0, r.dZ, r.tnear, r.tfar, a.cutoff_raw) * a.scale;
+    d = march<STORE>(V, occ, r.X0, r.dX, r.Y0, r.dY, r.Z0, r.dZ, r.tnear, r.tfar, a.cutoff_raw) * a.scale;
   out[(size_t)y * w + x] = fminf(fmaxf(d, 0.f), 1.f);
 }
 
@@ -387,6 +388,39 @@ __global__ void __launch_bounds__(RB) k_hdist_sad(const float* __restrict__ f, c
   }
 }
 
+// Occupancy of 8^3-voxel cells (see OCC in asc_internal.cuh): one thread per
+// cell takes the maximum over its trilinear support.
+template <int STORE>
+__global__ void k_occupancy(DevVolume V, float cutoff_raw, uint8_t* __restrict__ occ)
+{
+  const int bx = (V.nx + OCC - 1) / OCC, by = (V.ny + OCC - 1) / OCC, bz = (V.nz + OCC - 1) / OCC;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= bx * by * bz) return;
+  const int cx = c % bx, cy = (c / bx) % by, cz = c / (bx * by);
+  float mx = -1.0f;
+  for (int z = max(cz * OCC - 1, 0); z < min(cz * OCC + OCC + 1, V.nz); ++z)
+    for (int y = max(cy * OCC - 1, 0); y < min(cy * OCC + OCC + 1, V.ny); ++y)
+      for (int x = max(cx * OCC - 1, 0); x < min(cx * OCC + OCC + 1, V.nx); ++x) {
+        float lo, hi;
+        unpack<STORE>(V.pairs[(size_t)z * V.nx * V.ny + (size_t)y * V.nx + x], lo, hi);
+        mx = fmaxf(mx, lo);
+      }
+  occ[c] = mx > cutoff_raw ? 1 : 0;
+}
+
+int g_empty_skip = 1;
+
+void build_occupancy(const DevVolume& V, float cutoff_raw, uint8_t* occ, cudaStream_t s)
+{
+  int n = (int)occupancy_cells(V);
+  if (V.storage == ASC_STORE_BF16)
+    k_occupancy<ASC_STORE_BF16><<<(n + 127) / 128, 128, 0, s>>>(V, cutoff_raw, occ);
+  else if (V.storage == ASC_STORE_F16)
+    k_occupancy<ASC_STORE_F16><<<(n + 127) / 128, 128, 0, s>>>(V, cutoff_raw, occ);
+  else
+    k_occupancy<ASC_STORE_U16><<<(n + 127) / 128, 128, 0, s>>>(V, cutoff_raw, occ);
+}
+
 // ---------------------------------------------------------------- host side
 
 static bool tree_needed(unsigned n)
@@ -477,6 +511,15 @@ ASC_API const char* asc_status_string(int st)
 }
 
 ASC_API const char* asc_last_error(void) { return g_last_error.c_str(); }
+
+ASC_API int asc_set_option(int option, int value)
+{
+  if (option == ASC_OPT_EMPTY_SKIP) {
+    g_empty_skip = value != 0;
+    return ASC_OK;
+  }
+  return ASC_ERR_ARG;
+}
 
 ASC_API int asc_malloc(void** p, size_t bytes)
 {
@@ -650,6 +693,8 @@ ASC_API int asc_volume_create(const void* data, int W, int H, int D, int bps, co
   }
   if (mn[0] > mx[0] || mn[1] > mx[1] || mn[2] > mx[2]) return ASC_ERR_EMPTY;
   auto* v = new asc_volume_host();
+  v->occ = nullptr;
+  v->occ_cutoff = NAN;
   int dims[3] = {mx[0] - mn[0] + 1, mx[1] - mn[1] + 1, mx[2] - mn[2] + 1};
   float norm = bps == 8 ? 255.0f : 65535.0f;
   v->min_value = vmin / norm;
@@ -707,13 +752,14 @@ ASC_API int asc_volume_destroy(asc_volume vol)
   auto* v = (asc_volume_host*)vol;
   if (!v) return ASC_ERR_ARG;
   cudaFree(v->pairs);
+  if (v->occ) cudaFree(v->occ);
   delete v;
   return ASC_OK;
 }
 
 namespace asc {
-int raycast_launch(const DevVolume& V, const float* m12, const float* vp, float step, float intensity, float cutoff,
-                   float* out, int w, int h, cudaStream_t s)
+int raycast_launch(const DevVolume& V, const uint8_t* occ, const float* m12, const float* vp, float step,
+                   float intensity, float cutoff, float* out, int w, int h, cudaStream_t s)
 {
   RayArgs a;
   memcpy(a.m, m12, sizeof a.m);
@@ -724,11 +770,11 @@ int raycast_launch(const DevVolume& V, const float* m12, const float* vp, float 
   a.cutoff_raw = cutoff / V.norm;
   dim3 grid((w + 15) / 16, (h + 15) / 16);
   if (V.storage == ASC_STORE_BF16)
-    k_raycast<ASC_STORE_BF16><<<grid, 256, 0, s>>>(V, a, out, w, h);
+    k_raycast<ASC_STORE_BF16><<<grid, 256, 0, s>>>(V, occ, a, out, w, h);
   else if (V.storage == ASC_STORE_F16)
-    k_raycast<ASC_STORE_F16><<<grid, 256, 0, s>>>(V, a, out, w, h);
+    k_raycast<ASC_STORE_F16><<<grid, 256, 0, s>>>(V, occ, a, out, w, h);
   else
-    k_raycast<ASC_STORE_U16><<<grid, 256, 0, s>>>(V, a, out, w, h);
+    k_raycast<ASC_STORE_U16><<<grid, 256, 0, s>>>(V, occ, a, out, w, h);
   ASC_LAUNCH_CHECK();
   return ASC_OK;
 }
@@ -747,7 +793,18 @@ ASC_API int asc_raycast(asc_volume vol, const double imv[16], const float vp[4],
   }
   float m[12];
   fold_matrix(imv, v->inv_scale, v->inv_trans, m);
-  return raycast_launch(v->dev, m, vp, step, intensity, cutoff, out, w, h, S(stream));
+  const uint8_t* occ = nullptr;
+  if (g_empty_skip) {
+    const float cut = cutoff / v->dev.norm;
+    if (!v->occ) ASC_CUDA(cudaMalloc(&v->occ, occupancy_cells(v->dev)));
+    if (!(v->occ_cutoff == cut)) {
+      build_occupancy(v->dev, cut, v->occ, S(stream));
+      ASC_LAUNCH_CHECK();
+      v->occ_cutoff = cut;
+    }
+    occ = v->occ;
+  }
+  return raycast_launch(v->dev, occ, m, vp, step, intensity, cutoff, out, w, h, S(stream));
 }
 
 // ---- images ----

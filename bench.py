@@ -198,7 +198,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
-    ap.add_argument("--iters", type=int, default=50)
+    ap.add_argument("--iters", type=int, default=50, help="PSO iterations per step")
+    ap.add_argument("--particles", type=int, default=100, help="PSO particles per bone")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain per-pose sample")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end pass")
     args = ap.parse_args()
     ws, rank, local, pg = dist_setup()
     if args.impl == "reference":
@@ -211,7 +214,7 @@ def main():
     L.call("asc_set_device", local)
     sc = make_scene(seed=rank)
     vols = render_targets(sc)
-    eng = api.Engine(sc, max_items=300, volumes=vols)
+    eng = api.Engine(sc, max_items=3 * args.particles, volumes=vols)
     lib = L.load()
     stream = C.c_void_p()
     L.call("asc_stream_create", C.byref(stream))
@@ -219,7 +222,7 @@ def main():
     L.call("asc_event_create", C.byref(ev0))
     L.call("asc_event_create", C.byref(ev1))
     flush = api.DeviceArray((256 << 20,), np.uint8)  # 256 MB > 129 MB L2
-    nb, npart, iters = 3, 100, args.iters
+    nb, npart, iters = 3, args.particles, args.iters
     best = np.zeros((nb, 6))
     bcost = np.zeros(nb)
     ev = C.c_longlong()
@@ -263,13 +266,13 @@ def main():
     barrier(pg)
     L.call("asc_device_sync")
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(0 if args.no_e2e else args.steps):
         for vi, p in enumerate(pinned):
             L.call("asc_image_update", eng.rads[vi].handle, p, stream)
         step()  # returns after the D2H copy of best poses and costs
     L.call("asc_device_sync")
     e2e_s = allmax(pg, (time.perf_counter() - t0) / args.steps)
-    e2e = ws * evals_per_step / e2e_s
+    e2e = ws * evals_per_step / e2e_s if not args.no_e2e else None
     # ---- roofline of the dominant kernel (ray cast) on one PSO-iteration batch
     L.call("asc_engine_profile", eng.handle, 1)
     rng = np.random.default_rng(3)
@@ -298,12 +301,14 @@ def main():
         t = json.load(open(traffic_path))
         traffic = t.get("bytes_per_launch_scaled")
     # ---- plain per-pose drop-in form on the same GPU (sampled)
-    nplain = 60
-    pb, pm = bones[::5][:nplain], man[::5][:nplain]
-    eng.eval(pb[:2], pm[:2], plain=True)
-    t0 = time.perf_counter()
-    eng.eval(pb, pm, plain=True)
-    plain_v = nplain / (time.perf_counter() - t0)
+    plain_v = None
+    if not args.no_plain:
+        nplain = 60
+        pb, pm = bones[::5][:nplain], man[::5][:nplain]
+        eng.eval(pb[:2], pm[:2], plain=True)
+        t0 = time.perf_counter()
+        eng.eval(pb, pm, plain=True)
+        plain_v = nplain / (time.perf_counter() - t0)
     # ---- CPU baseline (oracle) on a bounded sample
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -323,7 +328,8 @@ def main():
                              "note": "algorithmic gather bytes (16 B/sample + 8 B/pixel), served from L1/L2"},
                 "kernel_ms": {"setup": phase[0], "ray": phase[1], "view": phase[2]},
                 "work": {"samples_per_batch": samples.value, "pixels_per_batch": pixels.value, "batch": nb * npart},
-                "plain": {"value": plain_v, "unit": "pose-evals/s", "speedup": value / plain_v},
+                "plain": {"value": plain_v, "unit": "pose-evals/s",
+                          "speedup": value / plain_v if plain_v else None},
                 "cpu_baseline": cpu, "clocks": clk.summary(),
                 "best_cost": bcost.tolist()}
         print(json.dumps(line), flush=True)

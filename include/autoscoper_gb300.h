@@ -48,6 +48,14 @@ typedef struct asc_volume_s *asc_volume;
 typedef struct asc_image_s *asc_image;
 typedef struct asc_engine_s *asc_engine;
 
+/* Options (asc_set_option).  ASC_OPT_EMPTY_SKIP (default 1): the ray march
+ * steps over runs of samples inside 8^3-voxel cells whose voxels are all at
+ * or below the cutoff.  Such samples add exactly nothing in the reference
+ * (RayCaster_kernels.cu:189), so results are identical either way; 0 reads
+ * every sample (for A/B checks). */
+#define ASC_OPT_EMPTY_SKIP 1
+int asc_set_option(int option, int value);
+
 const char *asc_version(void);
 const char *asc_status_string(int status);
 /* Last CUDA error text seen by the library on this thread ("" if none). */

@@ -164,6 +164,29 @@ def test_ncc_hdist(n, coverage):
     assert abs(got - ref) <= 1e-5 * max(1.0, abs(ref)), (got, ref)
 
 
+@pytest.mark.parametrize("storage", [L.ASC_STORE_U16, L.ASC_STORE_BF16])
+def test_empty_space_skip_is_exact(small, storage):
+    """Skipping cells whose voxels are all <= cutoff leaves every DRR pixel
+    bit-identical (the skipped samples add nothing)."""
+    sc, tr = small
+    dv = api.DeviceVolume(sc.volumes[0], storage)
+    rng = np.random.default_rng(8)
+    try:
+        for k in range(3):
+            pose = S.perturb(sc.truth[0], rng, 3.0, 20.0).astype(np.float64)
+            for vi in range(2):
+                ok, m, vp, w, h = tr.view_setup(0, vi, pose)
+                rp = sc.ray[vi][0]
+                for cut in (rp.cutoff, 0.0, 0.02):
+                    L.call("asc_set_option", 1, 1)
+                    a = api.raycast(dv, _imv(sc, vi, pose), vp, rp.step, rp.intensity, cut, w, h).to_host()
+                    L.call("asc_set_option", 1, 0)
+                    b = api.raycast(dv, _imv(sc, vi, pose), vp, rp.step, rp.intensity, cut, w, h).to_host()
+                    assert np.array_equal(a, b)
+    finally:
+        L.call("asc_set_option", 1, 1)
+
+
 def test_ncc_degenerate():
     z = api.DeviceArray.from_host(np.zeros(64, np.float32))
     one = api.DeviceArray.from_host(np.ones(64, np.float32))
