@@ -113,20 +113,25 @@ __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __rest
   while (t > tnear) {
     const float X = fmaf(t, dX, X0), Y = fmaf(t, dY, Y0), Z = fmaf(t, dZ, Z0);
     if (occ) {
-      const int cx = min(max(__float2int_rd((X - 0.5f) * (1.0f / OCC)), 0), bx - 1);
-      const int cy = min(max(__float2int_rd((Y - 0.5f) * (1.0f / OCC)), 0), by - 1);
-      const int cz = min(max(__float2int_rd((Z - 0.5f) * (1.0f / OCC)), 0), bz - 1);
+      // texel centres sit at integer coordinates, so the lower tap is
+      // floor(X) (or floor(X) - 1 at an integer X, see tap) and its cell
+      // floor(X / OCC)
+      const int cx = min(max(__float2int_rd(X * (1.0f / OCC)), 0), bx - 1);
+      const int cy = min(max(__float2int_rd(Y * (1.0f / OCC)), 0), by - 1);
+      const int cz = min(max(__float2int_rd(Z * (1.0f / OCC)), 0), bz - 1);
       if (!__ldg(occ + (cz * by + cy) * bx + cx)) {
-        // whole steps until the lower tap leaves the cell; t decreases, so a
-        // coordinate moves by -d per step
+        // whole steps during which the lower tap stays at least 1e-3 voxel
+        // inside the cell (well above FP32 rounding of the coordinates);
+        // t decreases, so a coordinate moves by -d per step
+        const float G = 1.0e-3f;
         float s = 3.0e38f;
-        if (dX > 0.f) s = fminf(s, (X - (OCC * cx + 0.5f)) / dX);
-        if (dX < 0.f) s = fminf(s, ((OCC * cx + OCC + 0.5f) - X) / -dX);
-        if (dY > 0.f) s = fminf(s, (Y - (OCC * cy + 0.5f)) / dY);
-        if (dY < 0.f) s = fminf(s, ((OCC * cy + OCC + 0.5f) - Y) / -dY);
-        if (dZ > 0.f) s = fminf(s, (Z - (OCC * cz + 0.5f)) / dZ);
-        if (dZ < 0.f) s = fminf(s, ((OCC * cz + OCC + 0.5f) - Z) / -dZ);
-        const float m = fminf(fmaxf(floorf(s - 0.01f), 0.f), 1.0e6f);
+        if (dX > 0.f) s = fminf(s, (X - (float)(OCC * cx) - G) / dX);
+        if (dX < 0.f) s = fminf(s, ((float)(OCC * cx + OCC) - X - G) / -dX);
+        if (dY > 0.f) s = fminf(s, (Y - (float)(OCC * cy) - G) / dY);
+        if (dY < 0.f) s = fminf(s, ((float)(OCC * cy + OCC) - Y - G) / -dY);
+        if (dZ > 0.f) s = fminf(s, (Z - (float)(OCC * cz) - G) / dZ);
+        if (dZ < 0.f) s = fminf(s, ((float)(OCC * cz + OCC) - Z - G) / -dZ);
+        const float m = fminf(fmaxf(floorf(s), 0.f), 1.0e6f);
         t -= m + 1.0f;
         continue;
       }

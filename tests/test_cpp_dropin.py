@@ -50,7 +50,14 @@ def test_dropin_matches_oracle(tmp_path):
     D, H, W = vol.data.shape
     spec = [W, H, D, 16, *vol.scale, str(tmp_path / "vol.raw"), *imv, *np.float32(vp), rp.step, rp.intensity,
             rp.cutoff, 96, 96, 16, str(tmp_path / "rad.raw"), *np.float32(v.camera.viewport), w, h, 1.0, 0.0]
-    (tmp_path / "spec.txt").write_text(" ".join(repr(float(x)) if not isinstance(x, str) else x for x in spec))
+    def fmt(x):
+        if isinstance(x, str):
+            return x
+        if isinstance(x, (int, np.integer)):
+            return str(int(x))
+        return repr(float(x))
+
+    (tmp_path / "spec.txt").write_text(" ".join(fmt(x) for x in spec))
     subprocess.run([exe, str(tmp_path / "spec.txt"), str(tmp_path / "out.bin")], check=True)
     raw = np.fromfile(tmp_path / "out.bin", np.uint8)
     n = w * h
