@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
 template <int STORE>
 __device__ __forceinline__ float march_any(const DevVolume& V, const uint8_t* occ, const RaySetup& r, float cut)
 {
-  return march<STORE>(V, occ, r.X0, r.dX, r.Y0, r.dY, r.Z0, r.dZ, r.tnear, r.tfar, cut);
+  return march<STORE>(V, occ, r, cut);
 }
 
 __global__ void __launch_bounds__(256) k_ray(const SceneDev* __restrict__ sc, Bufs b, int skip)
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(256) k_ray(const SceneDev* __restrict__ sc, Bu
     const bool hit = ray_setup(r.m, r.vp, x, y, r.w, r.h, B.step[v], B.vol.nx, B.vol.ny, B.vol.nz, rs);
     {
       // trilinear samples of this ray (the work figure of the roofline)
-      unsigned cnt = hit ? (unsigned)ceilf(rs.tfar - rs.tnear) : 0u;
+      unsigned cnt = hit ? (unsigned)rs.K : 0u;
       unsigned mask = __activemask();
       unsigned tot = __reduce_add_sync(mask, cnt);
       if ((int)(threadIdx.x & 31) == __ffs(mask) - 1) atomicAdd(&b.C->samples, (unsigned long long)tot);

@@ -93,54 +93,216 @@ __device__ __forceinline__ void tap(float X, int& k, float& a)
 // nothing to the DRR (RayCaster_kernels.cu:189); the march skips it.
 constexpr int OCC = 8;
 
-// One ray of cuda_volume_render_kernel (RayCaster_kernels.cu:144-195) from
-// t = far down to t > near in unit steps, sampling at voxel coordinates
-// (X0 + t dX, Y0 + t dY, Z0 + t dZ).  Returns the compensated (Kahan) sum of
+// ---- double-float arithmetic: a value is the unevaluated sum h + l of two
+// FP32 numbers (Dekker/Knuth error-free transformations with FMA), about 48
+// significant bits.  Used once per ray so that sample positions match FP64.
+struct df {
+  float h, l;
+};
+
+__device__ __forceinline__ df df_two_sum(float a, float b)
+{
+  const float s = __fadd_rn(a, b);
+  const float bb = __fadd_rn(s, -a);
+  return {s, __fadd_rn(__fadd_rn(a, -__fadd_rn(s, -bb)), __fadd_rn(b, -bb))};
+}
+
+__device__ __forceinline__ df df_fast(float a, float b)  // requires |a| >= |b|
+{
+  const float s = __fadd_rn(a, b);
+  return {s, __fadd_rn(b, -__fadd_rn(s, a))};
+}
+
+__device__ __forceinline__ df df_add(df a, df b)
+{
+  df s = df_two_sum(a.h, b.h);
+  const df t = df_two_sum(a.l, b.l);
+  s.l = __fadd_rn(s.l, t.h);
+  s = df_fast(s.h, s.l);
+  s.l = __fadd_rn(s.l, t.l);
+  return df_fast(s.h, s.l);
+}
+
+__device__ __forceinline__ df df_neg(df a) { return {-a.h, -a.l}; }
+
+__device__ __forceinline__ df df_mulf(df a, float b)
+{
+  const float p = __fmul_rn(a.h, b);
+  float e = fmaf(a.h, b, -p);
+  e = fmaf(a.l, b, e);
+  return df_fast(p, e);
+}
+
+__device__ __forceinline__ df df_mul(df a, df b)
+{
+  const float p = __fmul_rn(a.h, b.h);
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return df_fast(p, e);
+}
+
+__device__ __forceinline__ df df_div(df a, df b)
+{
+  const float q1 = __fdiv_rn(a.h, b.h);
+  df r = df_add(a, df_neg(df_mulf(b, q1)));
+  const float q2 = __fdiv_rn(r.h, b.h);
+  r = df_add(r, df_neg(df_mulf(b, q2)));
+  const float q3 = __fdiv_rn(r.h, b.h);
+  return df_add(df_fast(q1, q2), df{q3, 0.f});
+}
+
+__device__ __forceinline__ df df_sqrt(df a)
+{
+  const float s = __fsqrt_rn(a.h);
+  if (!(s > 0.f)) return {s, 0.f};
+  const df e = df_add(a, df_neg(df_mul(df{s, 0.f}, df{s, 0.f})));
+  return df_fast(s, __fdiv_rn(e.h, 2.0f * s));
+}
+
+__device__ __forceinline__ bool df_lt(df a, df b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
+
+// Per-ray set-up of cuda_volume_render_kernel (RayCaster_kernels.cu:144-186)
+// for pixel (x, y) of a w x h image over `vp`, with camera->volume matrix m
+// (3x4 row-major, normalisation folded), in double-float: the reference's
+// FP32 set-up misplaces the far intersection by ~1e-7 of its length, which
+// shifts every sample of the ray; here positions agree with FP64 to ~1e-6
+// voxel.  Sample k (k = 0 .. K-1) sits at t = far - k, texel coordinates
+// (X - k dX, Y - k dY, Z - k dZ) with texel centres at integers.
+struct RaySetup {
+  int K;
+  df X, Y, Z, dX, dY, dZ;
+};
+
+__device__ __forceinline__ bool ray_setup(const float* m, const float* vp, int x, int y, int w, int h, float step,
+                                          int nx, int ny, int nz, RaySetup& r)
+{
+  const df u = df_add(df{vp[0], 0.f}, df_mulf(df_div(df{(float)x, 0.f}, df{(float)w, 0.f}), vp[2]));
+  const df v = df_add(df{vp[1], 0.f}, df_mulf(df_div(df{(float)y, 0.f}, df{(float)h, 0.f}), vp[3]));
+  const df len = df_sqrt(df_add(df_add(df_mul(u, u), df_mul(v, v)), df{4.0f, 0.f}));
+  const df sc = df_div(df{step, 0.f}, len);
+  const df l0 = df_mul(u, sc), l1 = df_mul(v, sc), l2 = df_mulf(sc, -2.0f);
+  df d[3];
+  for (int i = 0; i < 3; ++i)
+    d[i] = df_add(df_add(df_mulf(l0, m[4 * i]), df_mulf(l1, m[4 * i + 1])), df_mulf(l2, m[4 * i + 2]));
+  const float o[3] = {m[3], m[7], m[11]};
+  const float lo[3] = {0.0f, 0.0f, -1.0f}, hi[3] = {1.0f, 1.0f, 0.0f};
+  df tn = {-3.0e38f, 0.f}, tf = {3.0e38f, 0.f};
+  for (int i = 0; i < 3; ++i) {
+    if (d[i].h == 0.f) {  // parallel to the slab
+      if (!(o[i] > lo[i] && o[i] < hi[i])) return false;
+      continue;
+    }
+    df a = df_div(df_two_sum(lo[i], -o[i]), d[i]);
+    df b = df_div(df_two_sum(hi[i], -o[i]), d[i]);
+    if (df_lt(b, a)) {
+      const df c = a;
+      a = b;
+      b = c;
+    }
+    if (df_lt(tn, a)) tn = a;
+    if (df_lt(b, tf)) tf = b;
+  }
+  if (!df_lt(tn, tf)) return false;  // also a miss for NaN
+  if (tn.h < 0.f) tn = df{0.f, 0.f};
+  // samples t = far - k > near: K = #{k >= 0 : k < far - near}
+  const df D = df_add(tf, df_neg(tn));
+  // t -= 1 stops making progress at 2^24; the reference would spin forever on
+  // such a degenerate ray, here it counts as a miss.
+  if (!(D.h < 8388608.0f)) return false;
+  if (D.h < 0.f || (D.h == 0.f && D.l <= 0.f)) {
+    r.K = 0;
+  } else {
+    const float c = ceilf(D.h);
+    r.K = (int)c + ((c == D.h && D.l > 0.f) ? 1 : 0);
+  }
+  // texture coordinates (p.x, 1 - p.y, -p.z) at t = far, minus the half texel
+  const df p0 = df_add(df{o[0], 0.f}, df_mul(tf, d[0]));
+  const df p1 = df_add(df{o[1], 0.f}, df_mul(tf, d[1]));
+  const df p2 = df_add(df{o[2], 0.f}, df_mul(tf, d[2]));
+  r.X = df_add(df_mulf(p0, (float)nx), df{-0.5f, 0.f});
+  r.Y = df_add(df_mulf(df_add(df{1.0f, 0.f}, df_neg(p1)), (float)ny), df{-0.5f, 0.f});
+  r.Z = df_add(df_mulf(df_neg(p2), (float)nz), df{-0.5f, 0.f});
+  r.dX = df_mulf(d[0], (float)nx);   // X decreases by dX per sample (t decreases)
+  r.dY = df_mulf(d[1], -(float)ny);
+  r.dZ = df_mulf(d[2], -(float)nz);
+  return true;
+}
+
+// Integer base and FP32 fraction of coordinate C - k dC (re-based every
+// RB samples so that the fraction stays small and exact to ~1e-6 voxel).
+constexpr float REBASE = 32.0f;
+__device__ __forceinline__ void coord_base(df C, df dC, float k, int& base_i, float& base_f, float& frac)
+{
+  const df c = df_add(C, df_neg(df_mulf(dC, k)));
+  const float fl = floorf(c.h);
+  base_f = fl;
+  base_i = (int)fminf(fmaxf(fl, -1.0e6f), 1.0e6f);
+  frac = __fadd_rn(__fadd_rn(c.h, -fl), c.l);
+}
+
+// One ray of cuda_volume_render_kernel (RayCaster_kernels.cu:187-195): the K
+// samples from t = far towards near.  Returns the compensated (Kahan) sum of
 // raw samples above cutoff_raw (the caller scales by step * norm /
 // intensity).  With `occ`, runs of samples inside empty cells are stepped
 // over without being read: the same samples contribute, in the same order.
 template <int STORE>
-__device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __restrict__ occ, float X0, float dX,
-                                       float Y0, float dY, float Z0, float dZ, float tnear, float tfar,
+__device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __restrict__ occ, const RaySetup& r,
                                        float cutoff_raw)
 {
   const uint32_t* __restrict__ P = V.pairs;
   const int nx = V.nx, ny = V.ny, nz = V.nz;
   const int sxy = nx * ny;
   const int bx = (nx + OCC - 1) / OCC, by = (ny + OCC - 1) / OCC, bz = (nz + OCC - 1) / OCC;
+  const float dXh = r.dX.h, dXl = r.dX.l, dYh = r.dY.h, dYl = r.dY.l, dZh = r.dZ.h, dZl = r.dZ.l;
   float acc = 0.f, comp = 0.f;
-  float t = tfar;
-  while (t > tnear) {
-    const float X = fmaf(t, dX, X0), Y = fmaf(t, dY, Y0), Z = fmaf(t, dZ, Z0);
+  int bix = 0, biy = 0, biz = 0;
+  float bfx = 0.f, bfy = 0.f, bfz = 0.f, fx = 0.f, fy = 0.f, fz = 0.f;
+  float j = REBASE;  // samples since the last base
+  for (int k = 0; k < r.K;) {
+    if (j >= REBASE) {
+      const float kf = (float)k;
+      coord_base(r.X, r.dX, kf, bix, bfx, fx);
+      coord_base(r.Y, r.dY, kf, biy, bfy, fy);
+      coord_base(r.Z, r.dZ, kf, biz, bfz, fz);
+      j = 0.f;
+    }
+    const float FX = fmaf(-j, dXh, fmaf(-j, dXl, fx));
+    const float FY = fmaf(-j, dYh, fmaf(-j, dYl, fy));
+    const float FZ = fmaf(-j, dZh, fmaf(-j, dZl, fz));
     if (occ) {
-      // texel centres sit at integer coordinates, so the lower tap is
-      // floor(X) (or floor(X) - 1 at an integer X, see tap) and its cell
-      // floor(X / OCC)
+      // the lower tap is floor(X) (or floor(X) - 1 at an integer X, see tap)
+      // and its cell floor(X / OCC); X here is approximate (~1e-5 voxel)
+      const float X = bfx + FX, Y = bfy + FY, Z = bfz + FZ;
       const int cx = min(max(__float2int_rd(X * (1.0f / OCC)), 0), bx - 1);
       const int cy = min(max(__float2int_rd(Y * (1.0f / OCC)), 0), by - 1);
       const int cz = min(max(__float2int_rd(Z * (1.0f / OCC)), 0), bz - 1);
       if (!__ldg(occ + (cz * by + cy) * bx + cx)) {
-        // whole steps during which the lower tap stays at least 1e-3 voxel
-        // inside the cell (well above FP32 rounding of the coordinates);
-        // t decreases, so a coordinate moves by -d per step
+        // whole samples during which the lower tap stays at least 1e-3 voxel
+        // inside the cell (well above the error of X); a coordinate moves by
+        // -d per sample
         const float G = 1.0e-3f;
         float s = 3.0e38f;
-        if (dX > 0.f) s = fminf(s, (X - (float)(OCC * cx) - G) / dX);
-        if (dX < 0.f) s = fminf(s, ((float)(OCC * cx + OCC) - X - G) / -dX);
-        if (dY > 0.f) s = fminf(s, (Y - (float)(OCC * cy) - G) / dY);
-        if (dY < 0.f) s = fminf(s, ((float)(OCC * cy + OCC) - Y - G) / -dY);
-        if (dZ > 0.f) s = fminf(s, (Z - (float)(OCC * cz) - G) / dZ);
-        if (dZ < 0.f) s = fminf(s, ((float)(OCC * cz + OCC) - Z - G) / -dZ);
-        const float m = fminf(fmaxf(floorf(s), 0.f), 1.0e6f);
-        t -= m + 1.0f;
+        if (dXh > 0.f) s = fminf(s, (X - (float)(OCC * cx) - G) / dXh);
+        if (dXh < 0.f) s = fminf(s, ((float)(OCC * cx + OCC) - X - G) / -dXh);
+        if (dYh > 0.f) s = fminf(s, (Y - (float)(OCC * cy) - G) / dYh);
+        if (dYh < 0.f) s = fminf(s, ((float)(OCC * cy + OCC) - Y - G) / -dYh);
+        if (dZh > 0.f) s = fminf(s, (Z - (float)(OCC * cz) - G) / dZh);
+        if (dZh < 0.f) s = fminf(s, ((float)(OCC * cz + OCC) - Z - G) / -dZh);
+        const float m = fminf(fmaxf(floorf(s), 0.f), 1.0e6f) + 1.0f;
+        k += (int)m;
+        j += m;
         continue;
       }
     }
     int ix, iy, iz;
     float ax, ay, az;
-    tap(X, ix, ax);
-    tap(Y, iy, ay);
-    tap(Z, iz, az);
+    tap(FX, ix, ax);
+    tap(FY, iy, ay);
+    tap(FZ, iz, az);
+    ix += bix;
+    iy += biy;
+    iz += biz;
     // clamp-to-edge; below the first texel both taps are texel 0
     if (ix < 0) { ix = 0; ax = 0.f; }
     ix = min(ix, nx - 1);
@@ -173,7 +335,8 @@ __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __rest
       comp = (tt - acc) - y;
       acc = tt;
     }
-    t -= 1.0f;
+    ++k;
+    j += 1.0f;
   }
   return acc;
 }
@@ -187,46 +350,6 @@ inline size_t occupancy_cells(const DevVolume& V)
 
 // Global switches (asc_set_option).
 extern int g_empty_skip;
-
-// Per-ray set-up of cuda_volume_render_kernel: pixel (x, y) of a w x h image
-// over `vp`, camera->volume matrix m (3x4 row-major, normalisation folded).
-// Returns false when the ray misses the unit box [0,1]x[0,1]x[-1,0].
-struct RaySetup {
-  float X0, dX, Y0, dY, Z0, dZ, tnear, tfar;
-};
-
-__device__ __forceinline__ bool ray_setup(const float* m, const float* vp, int x, int y, int w, int h, float step,
-                                          int nx, int ny, int nz, RaySetup& r)
-{
-  float u = vp[0] + vp[2] * (x / (float)w);
-  float v = vp[1] + vp[3] * (y / (float)h);
-  float inv = step / sqrtf(u * u + v * v + 4.0f);
-  float lx = u * inv, ly = v * inv, lz = -2.0f * inv;
-  float ox = m[3], oy = m[7], oz = m[11];
-  float dx = m[0] * lx + m[1] * ly + m[2] * lz;
-  float dy = m[4] * lx + m[5] * ly + m[6] * lz;
-  float dz = m[8] * lx + m[9] * ly + m[10] * lz;
-  float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
-  float bx = ix * (0.0f - ox), tx = ix * (1.0f - ox);
-  float by = iy * (0.0f - oy), ty = iy * (1.0f - oy);
-  float bz = iz * (-1.0f - oz), tz = iz * (0.0f - oz);
-  float tn = fmaxf(fmaxf(fminf(tx, bx), fminf(ty, by)), fminf(tz, bz));
-  float tf = fminf(fminf(fmaxf(tx, bx), fmaxf(ty, by)), fmaxf(tz, bz));
-  if (!(tf > tn)) return false;
-  // t -= 1 stops making progress at 2^24; the reference would spin forever on
-  // such a degenerate ray, here it counts as a miss.
-  if (!(tf < 8388608.0f)) return false;
-  r.tnear = tn < 0.0f ? 0.0f : tn;
-  r.tfar = tf;
-  // texture coordinates (p.x, 1 - p.y, -p.z) in texel units
-  r.X0 = ox * nx - 0.5f;
-  r.dX = dx * nx;
-  r.Y0 = (1.0f - oy) * ny - 0.5f;
-  r.dY = -dy * ny;
-  r.Z0 = -oz * nz - 0.5f;
-  r.dZ = -dz * nz;
-  return true;
-}
 
 // Bilinear read of an 8/16-bit (normalized) or float image with normalized
 // coordinates and clamp-to-edge, as tex2D<float> with the reference's

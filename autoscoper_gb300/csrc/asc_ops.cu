@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(256) k_raycast(DevVolume V, const uint8_t* __r
   RaySetup r;
   float d = 0.f;
   if (ray_setup(a.m, a.vp, x, y, w, h, a.step, V.nx, V.ny, V.nz, r))
-    d = march<STORE>(V, occ, r.X0, r.dX, r.Y0, r.dY, r.Z0, r.dZ, r.tnear, r.tfar, a.cutoff_raw) * a.scale;
+    d = march<STORE>(V, occ, r, a.cutoff_raw) * a.scale;
   out[(size_t)y * w + x] = fminf(fmaxf(d, 0.f), 1.f);
 }
 
