@@ -20,6 +20,7 @@ namespace asc {
 static thread_local std::string g_last_error;
 
 void set_cuda_error(cudaError_t e) { g_last_error = cudaGetErrorString(e); }
+void set_error_message(const char* msg) { g_last_error = msg; }
 
 int cuda_status(cudaError_t e)
 {
@@ -423,7 +424,7 @@ void build_occupancy(const DevVolume& V, float cutoff_raw, uint8_t* occ, cudaStr
 
 // ---------------------------------------------------------------- host side
 
-static bool tree_needed(unsigned n)
+bool tree_needed(unsigned n)
 {
   while (n > 1) {
     unsigned T = n < 256u ? n : 256u;

@@ -1,0 +1,68 @@
+// The DRR ray march of the CUDA kernels (asc_march.cuh) compiled as host
+// C++: lets CPU tests check the kernel's own ray set-up, sample positions,
+// empty-cell skipping and accumulation against the FP64 oracle.
+#include <vector>
+
+#include "host_march_shim.h"
+#include "../../include/autoscoper_gb300.h"
+#include "../../autoscoper_gb300/csrc/asc_march.cuh"
+
+using namespace asc;
+
+static uint16_t to_bf16(unsigned v)
+{
+  uint32_t b;
+  float f = (float)v;
+  std::memcpy(&b, &f, 4);
+  b += 0x7fffu + ((b >> 16) & 1u);  // round to nearest even
+  return (uint16_t)(b >> 16);
+}
+
+extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int storage, int skip, const float* m,
+                          const float* vp, float step, float intensity, float cutoff, float* out, int w, int h,
+                          int* nsamples)
+{
+  if (storage != ASC_STORE_U16 && storage != ASC_STORE_BF16) return -1;
+  std::vector<uint32_t> pairs((size_t)nx * ny * nz);
+  for (size_t r = 0; r < (size_t)ny * nz; ++r)
+    for (int x = 0; x < nx; ++x) {
+      unsigned lo = vol[r * nx + x], hi = vol[r * nx + std::min(x + 1, nx - 1)];
+      if (storage == ASC_STORE_BF16) { lo = to_bf16(lo); hi = to_bf16(hi); }
+      pairs[r * nx + x] = lo | (hi << 16);
+    }
+  DevVolume V{pairs.data(), nx, ny, nz, storage, 1.0f / 65535.0f};
+  const float cut = cutoff / V.norm;
+  // occupancy as k_occupancy builds it
+  const int bx = (nx + OCC - 1) / OCC, by = (ny + OCC - 1) / OCC, bz = (nz + OCC - 1) / OCC;
+  std::vector<uint8_t> occ((size_t)bx * by * bz);
+  for (int cz = 0; cz < bz; ++cz)
+    for (int cy = 0; cy < by; ++cy)
+      for (int cx = 0; cx < bx; ++cx) {
+        float mx = -1.0f;
+        for (int z = std::max(cz * OCC - 1, 0); z < std::min(cz * OCC + OCC + 1, nz); ++z)
+          for (int y = std::max(cy * OCC - 1, 0); y < std::min(cy * OCC + OCC + 1, ny); ++y)
+            for (int x = std::max(cx * OCC - 1, 0); x < std::min(cx * OCC + OCC + 1, nx); ++x) {
+              float lo, hi;
+              uint32_t wd = pairs[(size_t)z * nx * ny + (size_t)y * nx + x];
+              if (storage == ASC_STORE_BF16) unpack<ASC_STORE_BF16>(wd, lo, hi);
+              else unpack<ASC_STORE_U16>(wd, lo, hi);
+              mx = std::max(mx, lo);
+            }
+        occ[((size_t)cz * by + cy) * bx + cx] = mx > cut ? 1 : 0;
+      }
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      RaySetup r;
+      float d = 0.f;
+      int n = 0;
+      if (ray_setup(m, vp, x, y, w, h, step, nx, ny, nz, r)) {
+        const uint8_t* o = skip ? occ.data() : nullptr;
+        float acc = storage == ASC_STORE_BF16 ? march<ASC_STORE_BF16>(V, o, r, cut) : march<ASC_STORE_U16>(V, o, r, cut);
+        d = acc * (step * V.norm / intensity);
+        n = r.K;
+      }
+      out[y * w + x] = std::min(std::max(d, 0.f), 1.f);
+      nsamples[y * w + x] = n;
+    }
+  return 0;
+}

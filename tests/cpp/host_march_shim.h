@@ -1,0 +1,35 @@
+// Host stand-ins for the handful of CUDA intrinsics that the ray march
+// (autoscoper_gb300/csrc/asc_march.cuh) uses, so that the same source
+// compiles as host C++ for CPU tests.  Build with -ffp-contract=off.
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#define __device__
+#define __host__
+#define __forceinline__ inline
+using std::max;
+using std::min;
+inline float __fadd_rn(float a, float b) { volatile float r = a + b; return r; }
+inline float __fmul_rn(float a, float b) { volatile float r = a * b; return r; }
+inline float __fdiv_rn(float a, float b) { volatile float r = a / b; return r; }
+inline float __fsqrt_rn(float a) { return std::sqrt(a); }
+inline int __float_as_int(float f) { int i; std::memcpy(&i, &f, 4); return i; }
+inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
+inline int __float2int_rd(float f) { return (int)std::floor(f); }
+template <class T> inline T __ldg(const T* p) { return *p; }
+struct float2 { float x, y; };
+struct __half2_raw { unsigned short x, y; };
+struct __half2 { unsigned short x, y; };
+// IEEE binary16 -> binary32
+inline float host_half_to_float(unsigned short h)
+{
+  unsigned s = (h >> 15) & 1u, e = (h >> 10) & 31u, m = h & 1023u;
+  float v;
+  if (e == 0) v = (float)m * (1.0f / 16777216.0f);
+  else if (e == 31) v = m ? NAN : INFINITY;
+  else v = __uint_as_float(((e + 112u) << 23) | (m << 13));
+  return s ? -v : v;
+}
+inline float2 __half22float2(__half2 h) { return {host_half_to_float(h.x), host_half_to_float(h.y)}; }
