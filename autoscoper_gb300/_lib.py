@@ -79,6 +79,7 @@ SIGNATURES = {
     "asc_ncc_init": (i32, [C.c_uint]),
     "asc_ncc": (i32, [vp, vp, vp, C.c_uint, i32, vp, vp]),
     "asc_hdist": (i32, [vp, vp, vp, C.c_uint, i32, vp, vp]),
+    "asc_ncc_noalloc": (i32, [vp, vp, vp, C.c_uint, i32, vp, vp]),
     "asc_ncc_host": (i32, [vp, vp, vp, C.c_uint, i32, P(f64), vp]),
     "asc_hdist_host": (i32, [vp, vp, vp, C.c_uint, i32, P(f64), vp]),
     "asc_engine_create": (i32, [i32, P(ViewDesc), i32, P(BoneDesc), i32, i32, i32, i32, i32, P(vp)]),

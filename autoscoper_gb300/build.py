@@ -21,7 +21,7 @@ BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden", "--expt-relaxed-constexpr",
          "-I" + os.path.join(ROOT, "include")]
-SOURCES = ["asc_ops.cu", "asc_engine.cu", "asc_host.cu"]
+SOURCES = ["asc_ops.cu", "asc_engine.cu", "asc_host.cu", "asc_noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -166,6 +166,22 @@ int asc_ncc(const float *f, const float *g, const float *mask, unsigned n, int c
             void *stream);
 int asc_hdist(const float *f, const float *g, const float *mask, unsigned n, int coverage, double *result_dev,
               void *stream);
+/* NCC that allocates nothing.  No counterpart in the reference: for callers
+ * that cannot allocate device memory when they score (an application that
+ * owns a fixed device-memory budget and does not let a library grow it, or a
+ * latency-critical loop that cannot afford cudaMalloc's implicit device
+ * synchronisation).  Same arguments, kernel and result as asc_ncc, but the
+ * per-block partials live in a fixed array compiled into the library, which
+ * every GPU that loads the library holds until exit (about 288 KiB).
+ * n may be at most ASC_NOALLOC_MAX_N elements; larger n returns
+ * ASC_ERR_RANGE.  The first call on a device looks up the array's device
+ * address, so make that first call before any stream capture.  All calls on
+ * a device share the array: calls that overlap on the GPU (different
+ * streams, or a second call issued before the first has finished on another
+ * stream) race and must be serialised by the caller. */
+#define ASC_NOALLOC_MAX_N (1u << 24)
+int asc_ncc_noalloc(const float *f, const float *g, const float *mask, unsigned n, int coverage,
+                    double *result_dev, void *stream);
 /* Blocking convenience forms returning the value on the host (the
  * reference's float ncc(...) / hdist(...) signatures). */
 int asc_ncc_host(const float *f, const float *g, const float *mask, unsigned n, int coverage, double *result,
