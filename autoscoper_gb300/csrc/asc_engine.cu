@@ -74,6 +74,7 @@ struct SceneDev {
 struct IV {
   float m[12];
   float vp[4];
+  float sx[2], sy[2];  // vp[2] / w and vp[3] / h as double-floats
   int w, h, ok, bone;
   int rtx, rty, ftx, fty;
   long long pix;  // offset of this crop in the DRR buffer
@@ -168,6 +169,10 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
       r.w = (int)w;
       r.h = (int)h;
       for (int j = 0; j < 4; ++j) r.vp[j] = (float)vp[j];
+      if (w > 0 && h > 0) {
+        df_split((double)r.vp[2] / (double)w, r.sx[0], r.sx[1]);
+        df_split((double)r.vp[3] / (double)h, r.sy[0], r.sy[1]);
+      }
       if (w == 0 || h == 0) {
         vc = 1.0 - 1e5;  // degenerate NCC of an empty crop
       } else {
@@ -265,7 +270,8 @@ __global__ void __launch_bounds__(256) k_ray(const SceneDev* __restrict__ sc, Bu
     const int v = k % nv;
     RaySetup rs;
     float d = 0.f;
-    const bool hit = ray_setup(r.m, r.vp, x, y, r.w, r.h, B.step[v], B.vol.nx, B.vol.ny, B.vol.nz, rs);
+    const bool hit = ray_setup(r.m, r.vp, x, y, df{r.sx[0], r.sx[1]}, df{r.sy[0], r.sy[1]}, B.step[v], B.vol.nx,
+                               B.vol.ny, B.vol.nz, rs);
     {
       // trilinear samples of this ray (the work figure of the roofline)
       unsigned cnt = hit ? (unsigned)rs.K : 0u;

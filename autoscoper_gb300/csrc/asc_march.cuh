@@ -130,25 +130,50 @@ __device__ __forceinline__ df df_sqrt(df a)
 
 __device__ __forceinline__ bool df_lt(df a, df b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
 
+// 1/a and 1/sqrt(a) in double-float: one Newton step from the FP32 value
+// (relative error of the FP32 start squared, ~1e-13).
+__device__ __forceinline__ df df_rcp(df a)
+{
+  const float r = __frcp_rn(a.h);
+  const df e = df_add(df{1.0f, 0.f}, df_neg(df_mulf(a, r)));  // 1 - a r
+  return df_fast(r, __fmul_rn(r, e.h));
+}
+
+__device__ __forceinline__ df df_rsqrt(df a)
+{
+  const float r = rsqrtf(a.h);
+  const df r2 = df_mul(df{r, 0.f}, df{r, 0.f});
+  const df e = df_add(df{1.0f, 0.f}, df_neg(df_mul(a, r2)));  // 1 - a r^2
+  return df_fast(r, __fmul_rn(0.5f * r, e.h));
+}
+
+// A float value as a double-float from a double (host or device).
+__device__ __host__ __forceinline__ void df_split(double d, float& h, float& l)
+{
+  h = (float)d;
+  l = (float)(d - (double)h);
+}
+
 // Per-ray set-up of cuda_volume_render_kernel (RayCaster_kernels.cu:144-186)
-// for pixel (x, y) of a w x h image over `vp`, with camera->volume matrix m
-// (3x4 row-major, normalisation folded), in double-float: the reference's
+// for pixel (x, y) of an image over viewport `vp`, with camera->volume matrix
+// m (3x4 row-major, normalisation folded), in double-float: the reference's
 // FP32 set-up misplaces the far intersection by ~1e-7 of its length, which
 // shifts every sample of the ray; here positions agree with FP64 to ~1e-6
-// voxel.  Sample k (k = 0 .. K-1) sits at t = far - k, texel coordinates
-// (X - k dX, Y - k dY, Z - k dZ) with texel centres at integers.
+// voxel.  (sxh, sxl) and (syh, syl) are vp[2] / w and vp[3] / h as
+// double-floats, so that u = vp[0] + x vp[2] / w.  Sample k (k = 0 .. K-1)
+// sits at t = far - k, texel coordinates (X - k dX, Y - k dY, Z - k dZ) with
+// texel centres at integers.
 struct RaySetup {
   int K;
   df X, Y, Z, dX, dY, dZ;
 };
 
-__device__ __forceinline__ bool ray_setup(const float* m, const float* vp, int x, int y, int w, int h, float step,
+__device__ __forceinline__ bool ray_setup(const float* m, const float* vp, int x, int y, df sx, df sy, float step,
                                           int nx, int ny, int nz, RaySetup& r)
 {
-  const df u = df_add(df{vp[0], 0.f}, df_mulf(df_div(df{(float)x, 0.f}, df{(float)w, 0.f}), vp[2]));
-  const df v = df_add(df{vp[1], 0.f}, df_mulf(df_div(df{(float)y, 0.f}, df{(float)h, 0.f}), vp[3]));
-  const df len = df_sqrt(df_add(df_add(df_mul(u, u), df_mul(v, v)), df{4.0f, 0.f}));
-  const df sc = df_div(df{step, 0.f}, len);
+  const df u = df_add(df{vp[0], 0.f}, df_mulf(sx, (float)x));
+  const df v = df_add(df{vp[1], 0.f}, df_mulf(sy, (float)y));
+  const df sc = df_mulf(df_rsqrt(df_add(df_add(df_mul(u, u), df_mul(v, v)), df{4.0f, 0.f})), step);
   const df l0 = df_mul(u, sc), l1 = df_mul(v, sc), l2 = df_mulf(sc, -2.0f);
   df d[3];
   for (int i = 0; i < 3; ++i)
@@ -161,8 +186,9 @@ __device__ __forceinline__ bool ray_setup(const float* m, const float* vp, int x
       if (!(o[i] > lo[i] && o[i] < hi[i])) return false;
       continue;
     }
-    df a = df_div(df_two_sum(lo[i], -o[i]), d[i]);
-    df b = df_div(df_two_sum(hi[i], -o[i]), d[i]);
+    const df rd = df_rcp(d[i]);
+    df a = df_mul(df_two_sum(lo[i], -o[i]), rd);
+    df b = df_mul(df_two_sum(hi[i], -o[i]), rd);
     if (df_lt(b, a)) {
       const df c = a;
       a = b;
@@ -230,6 +256,7 @@ __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __rest
   float bfx = 0.f, bfy = 0.f, bfz = 0.f, fx = 0.f, fy = 0.f, fz = 0.f;
   int kb = -REBASE;  // index of the current base, a multiple of REBASE
   float j = 0.f;     // k - kb
+  int kj = 0;        // the k that j belongs to
   for (int k = 0; k < r.K;) {
     if (k - kb >= REBASE) {
       kb = k & ~(REBASE - 1);
@@ -237,7 +264,11 @@ __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __rest
       coord_base(r.X, r.dX, kf, bix, bfx, fx);
       coord_base(r.Y, r.dY, kf, biy, bfy, fy);
       coord_base(r.Z, r.dZ, kf, biz, bfz, fz);
+      kj = k - 1;  // force j below
+    }
+    if (kj != k) {  // after a base change or a hop
       j = (float)(k - kb);
+      kj = k;
     }
     const float FX = fmaf(-j, dXh, fmaf(-j, dXl, fx));
     const float FY = fmaf(-j, dYh, fmaf(-j, dYl, fy));
@@ -245,11 +276,13 @@ __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __rest
     if (occ) {
       // the lower tap is floor(X) (or floor(X) - 1 at an integer X, see tap)
       // and its cell floor(X / OCC); X here is approximate (~1e-5 voxel)
-      const float X = bfx + FX, Y = bfy + FY, Z = bfz + FZ;
-      const int cx = min(max(__float2int_rd(X * (1.0f / OCC)), 0), bx - 1);
-      const int cy = min(max(__float2int_rd(Y * (1.0f / OCC)), 0), by - 1);
-      const int cz = min(max(__float2int_rd(Z * (1.0f / OCC)), 0), bz - 1);
-      if (!__ldg(occ + (cz * by + cy) * bx + cx)) {
+      float X = bfx + FX, Y = bfy + FY, Z = bfz + FZ;
+      bool hopped = false;
+      for (;;) {
+        const int cx = min(max(__float2int_rd(X * (1.0f / OCC)), 0), bx - 1);
+        const int cy = min(max(__float2int_rd(Y * (1.0f / OCC)), 0), by - 1);
+        const int cz = min(max(__float2int_rd(Z * (1.0f / OCC)), 0), bz - 1);
+        if (__ldg(occ + (cz * by + cy) * bx + cx)) break;
         // whole samples during which the lower tap stays at least 1e-3 voxel
         // inside the cell (well above the error of X); a coordinate moves by
         // -d per sample
@@ -263,9 +296,15 @@ __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __rest
         if (dZh < 0.f) s = fminf(s, ((float)(OCC * cz + OCC) - Z - G) / -dZh);
         const float m = fminf(fmaxf(floorf(s), 0.f), 1.0e6f) + 1.0f;
         k += (int)m;
-        j += m;
-        continue;
+        hopped = true;
+        if (k >= r.K) break;
+        // the next cell is found from approximate coordinates; the sample
+        // itself is placed from its own base below
+        X = fmaf(-m, dXh, X);
+        Y = fmaf(-m, dYh, Y);
+        Z = fmaf(-m, dZh, Z);
       }
+      if (hopped) continue;  // re-base (if needed) and place sample k exactly
     }
     int ix, iy, iz;
     float ax, ay, az;
@@ -308,6 +347,7 @@ __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __rest
       acc = tt;
     }
     ++k;
+    ++kj;
     j += 1.0f;
   }
   return acc;

@@ -54,6 +54,7 @@ struct RayArgs {
   float m[12];
   float vp[4];
   float step, scale, cutoff_raw;
+  float sx[2], sy[2];  // vp[2] / w and vp[3] / h as double-floats
 };
 
 template <int STORE>
@@ -66,7 +67,7 @@ __global__ void __launch_bounds__(256) k_raycast(DevVolume V, const uint8_t* __r
   if (x >= w || y >= h) return;
   RaySetup r;
   float d = 0.f;
-  if (ray_setup(a.m, a.vp, x, y, w, h, a.step, V.nx, V.ny, V.nz, r))
+  if (ray_setup(a.m, a.vp, x, y, df{a.sx[0], a.sx[1]}, df{a.sy[0], a.sy[1]}, a.step, V.nx, V.ny, V.nz, r))
     d = march<STORE>(V, occ, r, a.cutoff_raw) * a.scale;
   out[(size_t)y * w + x] = fminf(fmaxf(d, 0.f), 1.f);
 }
@@ -769,6 +770,8 @@ int raycast_launch(const DevVolume& V, const uint8_t* occ, const float* m12, con
   // density = step * sum(norm * raw) / intensity; cutoff compares normalized samples
   a.scale = step * V.norm / intensity;
   a.cutoff_raw = cutoff / V.norm;
+  df_split((double)vp[2] / (double)w, a.sx[0], a.sx[1]);
+  df_split((double)vp[3] / (double)h, a.sy[0], a.sy[1]);
   dim3 grid((w + 15) / 16, (h + 15) / 16);
   if (V.storage == ASC_STORE_BF16)
     k_raycast<ASC_STORE_BF16><<<grid, 256, 0, s>>>(V, occ, a, out, w, h);

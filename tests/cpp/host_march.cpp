@@ -55,7 +55,10 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
       RaySetup r;
       float d = 0.f;
       int n = 0;
-      if (ray_setup(m, vp, x, y, w, h, step, nx, ny, nz, r)) {
+      df sx, sy;
+      df_split((double)vp[2] / (double)w, sx.h, sx.l);
+      df_split((double)vp[3] / (double)h, sy.h, sy.l);
+      if (ray_setup(m, vp, x, y, sx, sy, step, nx, ny, nz, r)) {
         const uint8_t* o = skip ? occ.data() : nullptr;
         float acc = storage == ASC_STORE_BF16 ? march<ASC_STORE_BF16>(V, o, r, cut) : march<ASC_STORE_U16>(V, o, r, cut);
         d = acc * (step * V.norm / intensity);

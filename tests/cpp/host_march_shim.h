@@ -15,6 +15,8 @@ inline float __fadd_rn(float a, float b) { volatile float r = a + b; return r; }
 inline float __fmul_rn(float a, float b) { volatile float r = a * b; return r; }
 inline float __fdiv_rn(float a, float b) { volatile float r = a / b; return r; }
 inline float __fsqrt_rn(float a) { return std::sqrt(a); }
+inline float __frcp_rn(float a) { volatile float r = 1.0f / a; return r; }
+inline float rsqrtf(float a) { volatile float r = 1.0f / std::sqrt(a); return r; }
 inline int __float_as_int(float f) { int i; std::memcpy(&i, &f, 4); return i; }
 inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline int __float2int_rd(float f) { return (int)std::floor(f); }
