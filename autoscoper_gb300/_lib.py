@@ -7,7 +7,7 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SO = os.path.join(HERE, "libautoscoper_gb300.so")
+SO = os.environ.get("ASC_LIB_PATH") or os.path.join(HERE, "libautoscoper_gb300.so")
 
 vp = C.c_void_p
 i32 = C.c_int
@@ -19,6 +19,12 @@ ASC_OK = 0
 ASC_STORE_U16, ASC_STORE_F16, ASC_STORE_BF16 = 0, 1, 2
 ASC_SUM_TREE, ASC_SUM_FULL = 0, 1
 COST_FN = C.CFUNCTYPE(f64, P(f64), vp)
+BATCH_COST_FN = C.CFUNCTYPE(i32, i32, P(i32), P(f64), P(f64), vp)
+
+
+class OptParams(C.Structure):
+    _fields_ = [("method", i32), ("n_particles", i32), ("n_iter", i32), ("w", f64), ("c1", f64), ("c2", f64),
+                ("lo", f64), ("hi", f64), ("seed", C.c_uint64), ("offsets", f64 * 6), ("ftol", f64)]
 
 
 class FilterDesc(C.Structure):
@@ -58,6 +64,7 @@ SIGNATURES = {
     "asc_event_destroy": (i32, [vp]),
     "asc_host_alloc": (i32, [P(vp), C.c_size_t]),
     "asc_host_free": (i32, [vp]),
+    "asc_mem_info": (i32, [P(C.c_size_t), P(C.c_size_t)]),
     "asc_volume_create": (i32, [vp, i32, i32, i32, i32, P(f64), P(i32), i32, P(vp)]),
     "asc_volume_info": (i32, [vp, P(f32), P(f32), P(f64), P(f32), P(f32), P(i32)]),
     "asc_volume_destroy": (i32, [vp]),
@@ -96,6 +103,8 @@ SIGNATURES = {
                              P(C.c_longlong), vp]),
     "asc_pso_sequential": (i32, [COST_FN, vp, i32, f32, f32, C.c_uint, C.c_uint, C.c_uint, P(f32), P(f32)]),
     "asc_amoeba": (i32, [COST_FN, vp, P(f64), P(f64), i32, f64, P(i32)]),
+    "asc_amoeba_batch": (i32, [BATCH_COST_FN, vp, i32, P(f64), P(f64), i32, f64, P(i32)]),
+    "asc_engine_optimize_frame": (i32, [vp, P(OptParams), P(f64), P(f64), P(C.c_longlong), vp]),
 }
 
 _LIB = None

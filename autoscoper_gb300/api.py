@@ -9,6 +9,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib as L
+from . import geometry as G
 from . import scene as S
 
 
@@ -184,6 +185,26 @@ def elementwise(name, *srcs, out=None):
     return o
 
 
+def render_targets(sc: S.Scene, volumes=None, noise=0.01):
+    """Synthetic radiographs on the GPU: for every view, 1 - (sum of the
+    bones' DRRs at their ground-truth poses), rendered at the radiograph's
+    texel centres, plus N(0, noise), quantised to u16.  Returns the device
+    volumes so callers can reuse them."""
+    vols = volumes or [DeviceVolume(v) for v in sc.volumes]
+    for vi, v in enumerate(sc.views):
+        cam = v.camera
+        acc = np.zeros((cam.height, cam.width))
+        for b, dv in enumerate(vols):
+            xc = G.from_xyzypr(sc.truth[b])
+            mv = G.mul(G.inverse(cam.frame), xc)
+            imv = G.row_matrix(G.inverse(mv))
+            rp = sc.ray[vi][b]
+            acc += raycast(dv, imv, S.target_viewport(cam), rp.step, rp.intensity, rp.cutoff, cam.width,
+                           cam.height).to_host()
+        v.radiograph = S.radiograph_from_drr(acc, seed=vi, noise=noise)
+    return vols
+
+
 # ---------------------------------------------------------------- engine
 
 def _filters(lst, arr):
@@ -275,6 +296,19 @@ class Engine:
                C.byref(ev), None)
         return best, cost, ev.value
 
+    def optimize_frame(self, method=0, n_particles=64, n_iter=30, w=0.7298, c1=1.4962, c2=1.4962, lo=-6.0, hi=6.0,
+                       seed=1, offsets=(0.1,) * 6, ftol=1e-3):
+        """Tracker::optimize for one frame, all bones (asc_engine_optimize_frame).
+        Returns (poses (n_bones, 6), costs (n_bones,), evaluations)."""
+        nb = len(self.scene.volumes)
+        p = L.OptParams(method, n_particles, n_iter, w, c1, c2, lo, hi, seed, (C.c_double * 6)(*offsets), ftol)
+        poses = np.zeros((nb, 6))
+        cost = np.zeros(nb)
+        ev = C.c_longlong()
+        L.call("asc_engine_optimize_frame", self.handle, C.byref(p), poses.ctypes.data_as(C.POINTER(C.c_double)),
+               cost.ctypes.data_as(C.POINTER(C.c_double)), C.byref(ev), None)
+        return poses, cost, ev.value
+
     def debug_layout(self, n):
         d, lay = C.c_void_p(), C.c_void_p()
         L.call("asc_engine_debug", self.handle, C.byref(d), C.byref(lay))
@@ -295,6 +329,27 @@ def pso_sequential(cost, n_particles=100, lo=-1.0, hi=1.0, epochs=50, stall=25, 
     val = C.c_float()
     L.call("asc_pso_sequential", cb, None, n_particles, lo, hi, epochs, stall, seed, pos, C.byref(val))
     return np.array(pos[:], np.float32), float(val.value)
+
+
+def amoeba_batch(batch_cost, P, Y, ftol=1e-3):
+    """Lock-step speculative AMOEBA over ns simplices (asc_amoeba_batch).
+    batch_cost(who: int array, X: (n, ndim)) -> (n,) values."""
+    P = np.ascontiguousarray(P, dtype=np.float64).copy()
+    Y = np.ascontiguousarray(Y, dtype=np.float64).copy()
+    ns, mp, ndim = P.shape
+
+    def cb(n, who, x, y, ctx):
+        w = np.array([who[i] for i in range(n)])
+        X = np.array([x[i] for i in range(n * ndim)]).reshape(n, ndim)
+        v = batch_cost(w, X)
+        for i in range(n):
+            y[i] = float(v[i])
+        return 0
+    fn = L.BATCH_COST_FN(cb)
+    it = (C.c_int * ns)()
+    L.call("asc_amoeba_batch", fn, None, ns, P.ctypes.data_as(C.POINTER(C.c_double)),
+           Y.ctypes.data_as(C.POINTER(C.c_double)), ndim, ftol, it)
+    return P, Y, np.array(it[:])
 
 
 def amoeba(cost, P, Y, ftol=1e-3):

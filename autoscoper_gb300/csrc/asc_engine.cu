@@ -249,7 +249,10 @@ __device__ __forceinline__ float march_any(const DevVolume& V, const uint8_t* oc
   return march<STORE>(V, occ, r, cut);
 }
 
-__global__ void __launch_bounds__(256) k_ray(const SceneDev* __restrict__ sc, Bufs b, int skip)
+#ifndef ASC_RAY_MINBLOCKS
+#define ASC_RAY_MINBLOCKS 4  // 4 x 256 threads resident per SM (<= 64 registers)
+#endif
+__global__ void __launch_bounds__(256, ASC_RAY_MINBLOCKS) k_ray(const SceneDev* __restrict__ sc, Bufs b, int skip)
 {
   __shared__ int s_tile;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -691,6 +694,12 @@ struct asc_engine_s {
   int sms = 152;
   bool prof = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // device PSO: swarm state, the captured iteration and a private stream
+  double* sw_buf = nullptr;
+  int* sw_iter = nullptr;
+  cudaGraphExec_t pso_exec = nullptr;
+  double pso_key[5] = {0, 0, 0, 0, 0};
+  cudaStream_t own_stream = nullptr;
   int* d_bone = nullptr;
   double* d_manip = nullptr;
   double* d_cost = nullptr;
@@ -706,6 +715,8 @@ struct asc_engine_s {
     for (void* p : allocs) cudaFree(p);
     for (cudaEvent_t x : ev)
       if (x) cudaEventDestroy(x);
+    if (pso_exec) cudaGraphExecDestroy(pso_exec);
+    if (own_stream) cudaStreamDestroy(own_stream);
   }
   template <class T>
   cudaError_t alloc(T*& p, size_t n)
@@ -997,57 +1008,56 @@ ASC_API int asc_engine_pso(asc_engine e, int np, int n_iter, double w, double c1
   const int nb = e->n_bones, n = nb * np;
   if (n > e->max_items) return ASC_ERR_RANGE;
   cudaStream_t s = S(stream);
-  bool own = false;
-  if (!s) {
-    ASC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    own = true;
+  if (!s) {  // one private non-blocking stream per engine
+    if (!e->own_stream) ASC_CUDA(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
+    s = e->own_stream;
+  }
+  // swarm state: allocated once per engine, sized for max_items particles
+  if (!e->sw_buf) {
+    const size_t cap = (size_t)e->max_items, nbm = (size_t)e->n_bones;
+    cudaError_t err = e->alloc(e->sw_buf, cap * 6 * 3 + cap + nbm * 6 + nbm);
+    if (!err) err = e->alloc(e->sw_iter, 1);
+    if (err) return cuda_status(err);
   }
   Swarm sw;
-  double* buf = nullptr;
-  int* ibuf = nullptr;
-  size_t nd = (size_t)n * 6 * 3 + n + nb * 6 + nb;
-  cudaError_t err = cudaMalloc(&buf, nd * sizeof(double));
-  if (!err) err = cudaMalloc(&ibuf, sizeof(int));
-  if (err) {
-    if (buf) cudaFree(buf);
-    if (own) cudaStreamDestroy(s);
-    return cuda_status(err);
-  }
-  sw.x = buf;
+  sw.x = e->sw_buf;
   sw.v = sw.x + (size_t)n * 6;
   sw.pbx = sw.v + (size_t)n * 6;
   sw.pbc = sw.pbx + (size_t)n * 6;
   sw.gx = sw.pbc + n;
   sw.gc = sw.gx + nb * 6;
-  sw.iter = ibuf;
+  sw.iter = e->sw_iter;
   sw.bone = e->d_bone;
   sw.manip = e->d_manip;
-  int rc = ASC_OK;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  int tb = 128, gb = (n + tb - 1) / tb;
+  const int tb = 128, gb = (n + tb - 1) / tb;
   k_pso_init<<<gb, tb, 0, s>>>(sw, nb, np, lo, hi, seed);
-  err = cudaGetLastError();
-  if (!err) err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-  if (!err) {
-    k_pso_update<<<gb, tb, 0, s>>>(sw, nb, np, w, c1, c2, seed);
-    engine_launch(e, n, e->d_bone, e->d_manip, e->d_cost, nullptr, s, true);
-    k_pso_best<<<nb, 256, 0, s>>>(sw, nb, np, e->d_cost);
-    err = cudaStreamEndCapture(s, &graph);
+  cudaError_t err = cudaGetLastError();
+  // one iteration = update -> setup -> ray -> view -> best, captured once per
+  // (particles, w, c1, c2, seed) and replayed n_iter times
+  const double key[5] = {(double)np, w, c1, c2, (double)seed};
+  if (!err && (!e->pso_exec || memcmp(key, e->pso_key, sizeof key) != 0)) {
+    if (e->pso_exec) {
+      cudaGraphExecDestroy(e->pso_exec);
+      e->pso_exec = nullptr;
+    }
+    cudaGraph_t graph = nullptr;
+    err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (!err) {
+      k_pso_update<<<gb, tb, 0, s>>>(sw, nb, np, w, c1, c2, seed);
+      engine_launch(e, n, e->d_bone, e->d_manip, e->d_cost, nullptr, s, true);
+      k_pso_best<<<nb, 256, 0, s>>>(sw, nb, np, e->d_cost);
+      err = cudaStreamEndCapture(s, &graph);
+    }
+    if (!err) err = cudaGraphInstantiate(&e->pso_exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (!err) memcpy(e->pso_key, key, sizeof key);
   }
-  if (!err) err = cudaGraphInstantiate(&exec, graph, 0);
-  for (int it = 0; !err && it < n_iter; ++it) err = cudaGraphLaunch(exec, s);
+  for (int it = 0; !err && it < n_iter; ++it) err = cudaGraphLaunch(e->pso_exec, s);
   if (!err) err = cudaMemcpyAsync(best_manip, sw.gx, nb * 6 * sizeof(double), cudaMemcpyDeviceToHost, s);
   if (!err) err = cudaMemcpyAsync(best_cost, sw.gc, nb * sizeof(double), cudaMemcpyDeviceToHost, s);
   if (!err) err = cudaStreamSynchronize(s);
-  if (err) rc = cuda_status(err);
-  if (exec) cudaGraphExecDestroy(exec);
-  if (graph) cudaGraphDestroy(graph);
-  cudaFree(buf);
-  cudaFree(ibuf);
-  if (own) cudaStreamDestroy(s);
   if (evals) *evals = (long long)n * n_iter;
-  return rc;
+  return err ? cuda_status(err) : ASC_OK;
 }
 
 // ---------------------------------------------------------------- plain path
@@ -1144,5 +1154,112 @@ ASC_API int asc_engine_eval_plain(asc_engine e, int n, const int* bone, const do
     }
     cost[it] = total < 0 ? 9999.0 : total;
   }
+  return ASC_OK;
+}
+
+// ---------------------------------------------------------------- Tracker::optimize
+namespace {
+
+struct EvalCtx {
+  asc_engine e;
+  cudaStream_t s;
+  long long evals;
+};
+
+// Batch cost for asc_amoeba_batch: candidate i belongs to simplex (bone) who[i].
+int engine_batch_cost(int n, const int* who, const double* x, double* y, void* ctx)
+{
+  EvalCtx* c = (EvalCtx*)ctx;
+  const int cap = c->e->max_items;
+  for (int i0 = 0; i0 < n; i0 += cap) {
+    const int m = std::min(cap, n - i0);
+    int rc = asc_engine_eval_host(c->e, m, who + i0, x + 6 * (size_t)i0, y + i0, nullptr, c->s);
+    if (rc) return rc;
+  }
+  c->evals += n;
+  return ASC_OK;
+}
+
+// The pose after a manipulator, rounded to float as the reference's key
+// curves store it (Tracker.cpp:479-491, :558-571).
+void apply_manip(const BoneDev& B, const double* manip, double* out)
+{
+  double base[12], man[12], t1[12], t2[12];
+  frame_from_xyzypr(B.base, base);
+  frame_from_axis_angle(manip, man);
+  frame_mul(base, B.pivot_inv, t1);
+  frame_mul(t1, man, t2);
+  frame_mul(t2, B.pivot, t1);
+  frame_to_xyzypr(t1, out);
+  for (int i = 0; i < 6; ++i) out[i] = (double)(float)out[i];
+}
+
+}  // namespace
+
+ASC_API int asc_engine_optimize_frame(asc_engine e, const asc_opt_params* p, double* pose_out, double* cost_out,
+                                      long long* evals_out, void* stream)
+{
+  if (!e || !p || !pose_out) return ASC_ERR_ARG;
+  const int nb = e->n_bones;
+  if (nb * 7 > e->max_items) return ASC_ERR_RANGE;
+  cudaStream_t s = S(stream);
+  if (!s) {  // the engine's private stream, so that engines on other threads overlap
+    if (!e->own_stream) ASC_CUDA(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
+    s = e->own_stream;
+  }
+  EvalCtx ctx{e, s, 0};
+  std::vector<int> bones(nb);
+  for (int b = 0; b < nb; ++b) bones[b] = b;
+  // init_ncc = minimizationFunc(0) (Tracker.cpp:441-443)
+  std::vector<double> zero(6 * nb, 0.0), init(nb), fin(nb);
+  int rc = engine_batch_cost(nb, bones.data(), zero.data(), init.data(), &ctx);
+  if (rc) return rc;
+  if (p->method == 0) {
+    // PSO, then move the pose to the swarm's best (Tracker.cpp:445-491)
+    std::vector<double> best(6 * nb), bc(nb);
+    long long ev = 0;
+    rc = asc_engine_pso(e, p->n_particles, p->n_iter, p->w, p->c1, p->c2, p->lo, p->hi, p->seed, best.data(), bc.data(),
+                        &ev, (void*)s);
+    if (rc) return rc;
+    ctx.evals += ev;
+    for (int b = 0; b < nb; ++b) {
+      double np[6];
+      apply_manip(e->host.bones[b], best.data() + 6 * b, np);
+      rc = asc_engine_set_base_pose(e, b, np);
+      if (rc) return rc;
+    }
+  }
+  // Downhill Simplex from the offsets (Tracker.cpp:493-515), all bones at once
+  const int mp = 7;
+  std::vector<double> P((size_t)nb * mp * 6, 0.0), Y((size_t)nb * mp);
+  std::vector<int> who((size_t)nb * mp);
+  for (int b = 0; b < nb; ++b)
+    for (int i = 0; i < mp; ++i) {
+      who[b * mp + i] = b;
+      if (i > 0) P[((size_t)b * mp + i) * 6 + (i - 1)] = p->offsets[i - 1];
+    }
+  rc = engine_batch_cost(nb * mp, who.data(), P.data(), Y.data(), &ctx);
+  if (rc) return rc;
+  std::vector<int> iters(nb);
+  rc = asc_amoeba_batch(engine_batch_cost, &ctx, nb, P.data(), Y.data(), 6, p->ftol, iters.data());
+  if (rc) return rc;
+  // final_ncc = minimizationFunc(P[1]); keep the start of the simplex if not better (Tracker.cpp:517-525)
+  std::vector<double> vert0(6 * nb);
+  for (int b = 0; b < nb; ++b)
+    for (int j = 0; j < 6; ++j) vert0[6 * b + j] = P[(size_t)b * mp * 6 + j];
+  rc = engine_batch_cost(nb, bones.data(), vert0.data(), fin.data(), &ctx);
+  if (rc) return rc;
+  for (int b = 0; b < nb; ++b) {
+    double manip[6] = {0, 0, 0, 0, 0, 0};
+    if (p->method != 0 || fin[b] < init[b])
+      for (int j = 0; j < 6; ++j) manip[j] = vert0[6 * b + j];
+    double np[6];
+    apply_manip(e->host.bones[b], manip, np);
+    rc = asc_engine_set_base_pose(e, b, np);
+    if (rc) return rc;
+    for (int j = 0; j < 6; ++j) pose_out[6 * b + j] = np[j];
+    if (cost_out) cost_out[b] = (p->method != 0 || fin[b] < init[b]) ? fin[b] : init[b];
+  }
+  if (evals_out) *evals_out = ctx.evals;
   return ASC_OK;
 }

@@ -61,6 +61,7 @@ __device__ __forceinline__ void tap(float X, int& k, float& a)
 // nothing to the DRR (RayCaster_kernels.cu:189); the march skips it.
 constexpr int OCC = 8;
 
+
 // ---- double-float arithmetic: a value is the unevaluated sum h + l of two
 // FP32 numbers (Dekker/Knuth error-free transformations with FMA), about 48
 // significant bits.  Used once per ray so that sample positions match FP64.
@@ -225,9 +226,12 @@ __device__ __forceinline__ bool ray_setup(const float* m, const float* vp, int x
 
 // Integer base and FP32 fraction of coordinate C - k dC.  The march re-bases
 // at every multiple of REBASE samples, so that the fraction stays small
-// (exact to ~1e-6 voxel) and a sample's coordinates depend on its index k
-// alone, whatever was skipped before it.
-constexpr int REBASE = 32;
+// (|fraction| < 1 + REBASE |d|, exact to a few 1e-6 voxel) and a sample's
+// coordinates depend on its index k alone, whatever was skipped before it.
+#ifndef ASC_REBASE
+#define ASC_REBASE 64
+#endif
+constexpr int REBASE = ASC_REBASE;
 __device__ __forceinline__ void coord_base(df C, df dC, float k, int& base_i, float& base_f, float& frac)
 {
   const df c = df_add(C, df_neg(df_mulf(dC, k)));
@@ -250,13 +254,18 @@ __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __rest
   const int nx = V.nx, ny = V.ny, nz = V.nz;
   const int sxy = nx * ny;
   const int bx = (nx + OCC - 1) / OCC, by = (ny + OCC - 1) / OCC, bz = (nz + OCC - 1) / OCC;
-  const float dXh = r.dX.h, dXl = r.dX.l, dYh = r.dY.h, dYl = r.dY.l, dZh = r.dZ.h, dZl = r.dZ.l;
+  const float dXh = r.dX.h, dYh = r.dY.h, dZh = r.dZ.h;
+  // per-sample change of the coordinates, and its reciprocal for the
+  // cell-exit distances (only the sign and a 1e-3 voxel margin matter there)
+  const float iX = dXh != 0.f ? 1.0f / dXh : 0.f, iY = dYh != 0.f ? 1.0f / dYh : 0.f;
+  const float iZ = dZh != 0.f ? 1.0f / dZh : 0.f;
   float acc = 0.f, comp = 0.f;
   int bix = 0, biy = 0, biz = 0;
   float bfx = 0.f, bfy = 0.f, bfz = 0.f, fx = 0.f, fy = 0.f, fz = 0.f;
   int kb = -REBASE;  // index of the current base, a multiple of REBASE
   float j = 0.f;     // k - kb
   int kj = 0;        // the k that j belongs to
+  int inside = 0;    // samples from k on known to lie in an occupied cell
   for (int k = 0; k < r.K;) {
     if (k - kb >= REBASE) {
       kb = k & ~(REBASE - 1);
@@ -266,45 +275,36 @@ __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __rest
       coord_base(r.Z, r.dZ, kf, biz, bfz, fz);
       kj = k - 1;  // force j below
     }
-    if (kj != k) {  // after a base change or a hop
+    if (kj != k) {  // after a base change or a skip
       j = (float)(k - kb);
       kj = k;
     }
-    const float FX = fmaf(-j, dXh, fmaf(-j, dXl, fx));
-    const float FY = fmaf(-j, dYh, fmaf(-j, dYl, fy));
-    const float FZ = fmaf(-j, dZh, fmaf(-j, dZl, fz));
-    if (occ) {
+    // j * (low part of d) stays below 1e-6 voxel for j < REBASE
+    const float FX = fmaf(-j, dXh, fx), FY = fmaf(-j, dYh, fy), FZ = fmaf(-j, dZh, fz);
+    if (occ && inside <= 0) {
       // the lower tap is floor(X) (or floor(X) - 1 at an integer X, see tap)
       // and its cell floor(X / OCC); X here is approximate (~1e-5 voxel)
-      float X = bfx + FX, Y = bfy + FY, Z = bfz + FZ;
-      bool hopped = false;
-      for (;;) {
-        const int cx = min(max(__float2int_rd(X * (1.0f / OCC)), 0), bx - 1);
-        const int cy = min(max(__float2int_rd(Y * (1.0f / OCC)), 0), by - 1);
-        const int cz = min(max(__float2int_rd(Z * (1.0f / OCC)), 0), bz - 1);
-        if (__ldg(occ + (cz * by + cy) * bx + cx)) break;
-        // whole samples during which the lower tap stays at least 1e-3 voxel
-        // inside the cell (well above the error of X); a coordinate moves by
-        // -d per sample
-        const float G = 1.0e-3f;
-        float s = 3.0e38f;
-        if (dXh > 0.f) s = fminf(s, (X - (float)(OCC * cx) - G) / dXh);
-        if (dXh < 0.f) s = fminf(s, ((float)(OCC * cx + OCC) - X - G) / -dXh);
-        if (dYh > 0.f) s = fminf(s, (Y - (float)(OCC * cy) - G) / dYh);
-        if (dYh < 0.f) s = fminf(s, ((float)(OCC * cy + OCC) - Y - G) / -dYh);
-        if (dZh > 0.f) s = fminf(s, (Z - (float)(OCC * cz) - G) / dZh);
-        if (dZh < 0.f) s = fminf(s, ((float)(OCC * cz + OCC) - Z - G) / -dZh);
-        const float m = fminf(fmaxf(floorf(s), 0.f), 1.0e6f) + 1.0f;
-        k += (int)m;
-        hopped = true;
-        if (k >= r.K) break;
-        // the next cell is found from approximate coordinates; the sample
-        // itself is placed from its own base below
-        X = fmaf(-m, dXh, X);
-        Y = fmaf(-m, dYh, Y);
-        Z = fmaf(-m, dZh, Z);
+      const float X = bfx + FX, Y = bfy + FY, Z = bfz + FZ;
+      const int cx = min(max(__float2int_rd(X * (1.0f / OCC)), 0), bx - 1);
+      const int cy = min(max(__float2int_rd(Y * (1.0f / OCC)), 0), by - 1);
+      const int cz = min(max(__float2int_rd(Z * (1.0f / OCC)), 0), bz - 1);
+      // whole samples after this one during which the lower tap stays at
+      // least 1e-3 voxel inside the cell (well above the error of X); a
+      // coordinate moves by -d per sample
+      const float G = 1.0e-3f;
+      float s = 3.0e38f;
+      if (dXh > 0.f) s = fminf(s, (X - (float)(OCC * cx) - G) * iX);
+      if (dXh < 0.f) s = fminf(s, (X - (float)(OCC * cx + OCC) + G) * iX);
+      if (dYh > 0.f) s = fminf(s, (Y - (float)(OCC * cy) - G) * iY);
+      if (dYh < 0.f) s = fminf(s, (Y - (float)(OCC * cy + OCC) + G) * iY);
+      if (dZh > 0.f) s = fminf(s, (Z - (float)(OCC * cz) - G) * iZ);
+      if (dZh < 0.f) s = fminf(s, (Z - (float)(OCC * cz + OCC) + G) * iZ);
+      const int m = (int)fminf(fmaxf(floorf(s), 0.f), 1.0e6f) + 1;  // this sample and the next m - 1
+      if (!__ldg(occ + (cz * by + cy) * bx + cx)) {
+        k += m;  // all of them add nothing
+        continue;
       }
-      if (hopped) continue;  // re-base (if needed) and place sample k exactly
+      inside = m;
     }
     int ix, iy, iz;
     float ax, ay, az;
@@ -348,6 +348,7 @@ __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __rest
     }
     ++k;
     ++kj;
+    --inside;
     j += 1.0f;
   }
   return acc;

@@ -610,6 +610,12 @@ ASC_API int asc_host_free(void* p)
   ASC_CUDA(cudaFreeHost(p));
   return ASC_OK;
 }
+ASC_API int asc_mem_info(size_t* free_bytes, size_t* total_bytes)
+{
+  if (!free_bytes || !total_bytes) return ASC_ERR_ARG;
+  ASC_CUDA(cudaMemGetInfo(free_bytes, total_bytes));
+  return ASC_OK;
+}
 
 // ---- volumes (VolumeDescription.cpp:152-305) ----
 template <class T>

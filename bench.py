@@ -43,19 +43,8 @@ def make_scene(seed=0):
 
 def render_targets(sc):
     """Radiographs = 1 - sum of the bones' DRRs at the ground truth (GPU)."""
-    from autoscoper_gb300 import api, geometry as G, scene as S
-    vols = [api.DeviceVolume(v) for v in sc.volumes]
-    for vi, v in enumerate(sc.views):
-        cam = v.camera
-        acc = np.zeros((cam.height, cam.width))
-        for b, dv in enumerate(vols):
-            xc = G.from_xyzypr(sc.truth[b])
-            mv = G.mul(G.inverse(cam.frame), xc)
-            imv = G.row_matrix(G.inverse(mv))
-            rp = sc.ray[vi][b]
-            acc += api.raycast(dv, imv, S.target_viewport(cam), rp.step, rp.intensity, rp.cutoff, cam.width,
-                               cam.height).to_host()
-        v.radiograph = S.radiograph_from_drr(acc, seed=vi)
+    from autoscoper_gb300 import api, scene as S
+    vols = api.render_targets(sc)
     rng = np.random.Generator(np.random.PCG64(99))
     sc.poses = [S.perturb(t, rng, 5.0, 5.0) for t in sc.truth]
     return vols
@@ -335,5 +324,128 @@ def main():
         print(json.dumps(line), flush=True)
 
 
+def sinusoid_trajectory(truth0, frames, fps=250.0, seed=0, rot_amp=20.0, trans_amp=10.0):
+    """Per-axis sinusoids (rotations +-rot_amp deg, translations +-trans_amp mm)
+    at frequencies U(0.5, 2) Hz with random phase, sampled at fps."""
+    rng = np.random.default_rng(seed)
+    f = rng.uniform(0.5, 2.0, 6)
+    ph = rng.uniform(0, 2 * np.pi, 6)
+    amp = np.array([trans_amp] * 3 + [rot_amp] * 3)
+    t = np.arange(frames)[:, None] / fps
+    return np.asarray(truth0)[None, :] + amp * np.sin(2 * np.pi * f * t + ph) - amp * np.sin(ph)
+
+
+def run_tracking(args):
+    """Sequence tracking: 2 bones (256x128x128, 192x192x160 u16 @0.4 mm), 2 views
+    of 1024^2, sinusoidal ground truth at 250 fps; every frame starts from the
+    previous frame's pose, PSO (64 x 30) then Downhill Simplex.  Radiographs and
+    volumes stay resident on the GPU; frames/s end to end."""
+    from autoscoper_gb300 import _lib as L, api, scene as S
+    L.load()
+    sc = S.make_scene([(128, 128, 256), (160, 192, 192)], 0.4, (1024, 1024), 0.3, filters="sobel", seed=4,
+                      bone_offsets=[(0.0, 0.0, -30.0), (0.0, 0.0, 30.0)], rot_range=10.0)
+    nf = args.frames
+    traj = [sinusoid_trajectory(t, nf, seed=11 + b) for b, t in enumerate(sc.truth)]
+    vols = [api.DeviceVolume(v) for v in sc.volumes]
+    images = []
+    for f in range(nf):
+        sc.truth = [traj[b][f] for b in range(2)]
+        api.render_targets(sc, volumes=vols)
+        images.append([api.DeviceImage(v.radiograph) for v in sc.views])
+    rng = np.random.default_rng(5)
+    sc.poses = [S.perturb(traj[b][0], rng, 1.0, 1.0) for b in range(2)]
+    eng = api.Engine(sc, max_items=2 * 64, volumes=vols, images=images[0])
+    errs, evals = [], 0
+    L.call("asc_device_sync")
+    t0 = time.perf_counter()
+    for f in range(nf):
+        for vi in range(2):
+            eng.set_radiograph(vi, images[f][vi])
+        poses, cost, ev = eng.optimize_frame(method=0, n_particles=64, n_iter=30, lo=-3.0, hi=3.0, seed=100 + f)
+        evals += ev
+        errs.append([np.abs(poses[b] - traj[b][f]) for b in range(2)])
+    dt = time.perf_counter() - t0
+    e = np.array(errs)  # frames x bones x 6
+    return {"workload": "sequence tracking", "metric": "frames/s (end to end, PSO 64x30 + simplex, 2 bones, 2 views)",
+            "value": nf / dt, "unit": "frames/s", "frames": nf, "pose_evals": evals, "pose_evals_per_s": evals / dt,
+            "mean_err_mm": float(e[:, :, :3].mean()), "max_err_mm": float(e[:, :, :3].max()),
+            "mean_err_deg": float(e[:, :, 3:].mean()), "max_err_deg": float(e[:, :, 3:].max()),
+            "data": "synthetic sinusoidal trajectory, 250 fps"}
+
+
+def run_serving(args):
+    """Poisson stream of mixed registration jobs: continuous batching (4 slots,
+    HBM budget 150 GB, subject volume cache) against the FIFO loop."""
+    from autoscoper_gb300 import _lib as L, api, serve
+    L.load()
+
+    def jobs():
+        rng = np.random.default_rng(17)
+        t, out = 0.0, []
+        subjects = [f"subject{i}" for i in range(max(2, args.jobs // 2))]
+        for i in range(args.jobs):
+            t += rng.exponential(1.0 / args.rate)
+            out.append(serve.make_job(i, rng, subjects[int(rng.integers(len(subjects)))], t, frames=(1, 5),
+                                      particles=(32, 128), iterations=10, render_targets=api.render_targets))
+        return out
+
+    res = {}
+    for name, slots in (("continuous", 4), ("fifo", 1)):
+        js = jobs()
+        summary = serve.Server(hbm_budget=150e9, slots=slots).serve(js, realtime=True)
+        res[name] = summary
+    c, f = res["continuous"], res["fifo"]
+    return {"workload": "serving", "metric": "sustained pose evals/s; p50/p99 job latency",
+            "value": c["pose_evals_per_s"], "unit": "pose-evals/s", "rate_jobs_per_s": args.rate,
+            "continuous": c, "fifo": f, "speedup_vs_fifo": c["pose_evals_per_s"] / max(f["pose_evals_per_s"], 1e-9),
+            "data": "synthetic mixed jobs: volumes 64^3-320^3 u16, viewports 256^2-1024^2, 1-4 bones, 1-3 views, "
+                    "1-5 frames, PSO 32-128 particles x 10 iterations"}
+
+
+def run_precision(args):
+    """Storage precision on the batched workload: u16, FP16 and BF16 volumes
+    (FP32 sampling, compensated FP32 partials, FP64 combine) against the FP64
+    oracle on a sample of candidates, with pose-evals/s per storage."""
+    from autoscoper_gb300 import _lib as L, api
+    from oracle import oracle as O
+    L.load()
+    sc = make_scene()
+    vols = render_targets(sc)
+    tr = O.Tracker(sc)
+    rng = np.random.default_rng(8)
+    n = 300
+    bones = np.repeat(np.arange(3), 100).astype(np.int32)
+    man = np.concatenate([rng.uniform(-5, 5, (n, 3)), rng.uniform(-5, 5, (n, 3))], 1)
+    sample = rng.choice(n, size=args.oracle_sample, replace=False)
+    ref = {int(k): [1.0 - c for c in tr.track_frame(int(bones[k]), tr.compose(int(bones[k]), man[k]))]
+           for k in sample}
+    out = {}
+    for name, st in (("u16", L.ASC_STORE_U16), ("f16", L.ASC_STORE_F16), ("bf16", L.ASC_STORE_BF16)):
+        eng = api.Engine(sc, max_items=n, storage=st)
+        cost, vcost = eng.eval(bones, man)
+        errs = [abs((1.0 - vcost[k, v]) - ref[k][v]) / max(abs(ref[k][v]), 1e-12) for k in ref for v in range(2)]
+        eng.eval(bones, man)
+        L.call("asc_device_sync")
+        t0 = time.perf_counter()
+        for _ in range(3):
+            eng.eval(bones, man)
+        dt = (time.perf_counter() - t0) / 3
+        out[name] = {"ncc_rel_err_max": float(np.max(errs)), "ncc_rel_err_median": float(np.median(errs)),
+                     "pose_evals_per_s": n / dt}
+    return {"workload": "precision", "metric": "NCC relative error vs FP64 oracle per volume storage",
+            "storage": out, "oracle_sample": int(args.oracle_sample), "data": "batched PSO workload, synthetic"}
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] in ("tracking", "serving", "precision"):
+        ap = argparse.ArgumentParser()
+        ap.add_argument("workload")
+        ap.add_argument("--frames", type=int, default=20)
+        ap.add_argument("--jobs", type=int, default=24)
+        ap.add_argument("--rate", type=float, default=2.0, help="mean job arrivals per second")
+        ap.add_argument("--oracle-sample", type=int, default=12)
+        a = ap.parse_args()
+        fn = {"tracking": run_tracking, "serving": run_serving, "precision": run_precision}[a.workload]
+        print(json.dumps(fn(a)), flush=True)
+    else:
+        main()

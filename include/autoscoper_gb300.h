@@ -81,6 +81,8 @@ int asc_event_elapsed(void *start, void *stop, float *ms);
 int asc_event_destroy(void *event);
 int asc_host_alloc(void **ptr, size_t bytes);
 int asc_host_free(void *ptr);
+/* Free and total device memory of the current device (cudaMemGetInfo). */
+int asc_mem_info(size_t *free_bytes, size_t *total_bytes);
 
 /* ---- volumes ----
  * replaces gpu::VolumeDescription::VolumeDescription(const Volume&)
@@ -260,6 +262,35 @@ int asc_engine_stats(asc_engine e, float ms[3], unsigned long long *samples, uns
  * bone) receive gBest.  evals_out (optional) the number of poses scored. */
 int asc_engine_pso(asc_engine e, int n_particles, int n_iter, double w, double c1, double c2, double lo, double hi,
                    uint64_t seed, double *best_manip, double *best_cost, long long *evals_out, void *stream);
+
+/* Many Nelder-Mead simplices in lock-step (AMOEBA, DownhillSimplex.cpp:39-172):
+ * each iteration evaluates, per simplex, the reflection and speculatively the
+ * expansion and both contraction points in one batch call, then applies
+ * AMOEBA's decision rules, so each simplex follows the sequential AMOEBA's
+ * trajectory exactly.  P: ns x (ndim+1) x ndim, Y: ns x (ndim+1) (in/out);
+ * cost(n, who, x, y, ctx) fills y[i] for point x[i*ndim..] of simplex who[i]. */
+typedef int (*asc_batch_cost_fn)(int n, const int *who, const double *x, double *y, void *ctx);
+int asc_amoeba_batch(asc_batch_cost_fn cost, void *ctx, int ns, double *P, double *Y, int ndim, double ftol,
+                     int *iterations);
+
+/* Tracker::optimize (Tracker.cpp:337-580) for one frame and every bone of
+ * an engine at once.  method 0: PSO (asc_engine_pso with the parameters
+ * below), the pose moved to the swarm's best, then Downhill Simplex from the
+ * offsets; method 1: Downhill Simplex only.  As in the reference, the
+ * simplex result is kept only if it beats the cost at the frame's start pose
+ * (method 0).  Poses are rounded to float as the reference's key curves store
+ * them.  The engine's base poses are updated; pose_out (6 per bone) and
+ * cost_out (per bone) receive them. */
+typedef struct {
+  int method;          /* 0 PSO + simplex, 1 simplex only */
+  int n_particles, n_iter;
+  double w, c1, c2, lo, hi;
+  uint64_t seed;
+  double offsets[6];   /* initial simplex offsets (Trial::offsets, default 0.1) */
+  double ftol;         /* 1e-3 in the reference */
+} asc_opt_params;
+int asc_engine_optimize_frame(asc_engine e, const asc_opt_params *params, double *pose_out, double *cost_out,
+                              long long *evals_out, void *stream);
 
 /* Reference-sequential PSO on the host (PSO.cpp:198-295, asynchronous gBest,
  * glibc rand() after srand(seed), omega 0.8 * 0.9^epoch, c1 = c2 = 1.5),

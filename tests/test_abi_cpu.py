@@ -80,3 +80,24 @@ def test_host_amoeba_matches_reference(lib):
     Pb, Yb = P.copy(), Y.copy()
     itb = O.amoeba(_quadratic, Pb, Yb, 1e-3)
     assert ita == itb and np.array_equal(Pa, Pb) and np.array_equal(Ya, Yb)
+
+
+def _quadratic_k(x, k):
+    t = np.array([0.3, -0.2, 0.1, 1.0, -0.5, 0.25]) * (1 + 0.3 * k)
+    return float(np.sum((np.asarray(x, dtype=np.float64) - t) ** 2 * (1 + 0.1 * np.arange(6))) + 0.01 * k)
+
+
+def test_batched_speculative_amoeba_follows_sequential_trajectories(lib):
+    """Lock-step speculative AMOEBA on 4 simplices = the reference AMOEBA on each."""
+    ns = 4
+    P = np.zeros((ns, 7, 6))
+    for k in range(ns):
+        for i in range(1, 7):
+            P[k, i, i - 1] = 0.1 * (k + 1)
+    Y = np.array([[_quadratic_k(p, k) for p in P[k]] for k in range(ns)])
+    Pb, Yb, its = api.amoeba_batch(lambda who, X: [_quadratic_k(x, k) for k, x in zip(who, X)], P, Y, 1e-3)
+    for k in range(ns):
+        Pk, Yk = P[k].copy(), Y[k].copy()
+        it = O.amoeba(lambda x, k=k: _quadratic_k(x, k), Pk, Yk, 1e-3)
+        assert it == its[k]
+        assert np.array_equal(Pk, Pb[k]) and np.array_equal(Yk, Yb[k])
