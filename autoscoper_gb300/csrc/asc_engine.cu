@@ -37,7 +37,7 @@ constexpr int MAX_VIEWS = 4;
 constexpr int MAX_BONES = 16;
 constexpr int MAX_FILTERS = 8;
 constexpr int VT = 32;   // k_view output tile edge
-constexpr int RT = 16;   // k_ray tile edge
+constexpr int RTX = 8, RTY = 4;  // k_ray work item: one warp, 8 x 4 rays
 
 struct FilterDev {
   int kind, K, R;
@@ -177,8 +177,8 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
         vc = 1.0 - 1e5;  // degenerate NCC of an empty crop
       } else {
         r.ok = 1;
-        r.rtx = (r.w + RT - 1) / RT;
-        r.rty = (r.h + RT - 1) / RT;
+        r.rtx = (r.w + RTX - 1) / RTX;
+        r.rty = (r.h + RTY - 1) / RTY;
         r.ftx = (r.w + VT - 1) / VT;
         r.fty = (r.h + VT - 1) / VT;
       }
@@ -246,7 +246,9 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
 template <int STORE>
 __device__ __forceinline__ float march_any(const DevVolume& V, const uint8_t* occ, const RaySetup& r, float cut)
 {
-  return march<STORE>(V, occ, r, cut);
+  int k0, k1;
+  if (!occupied_span(V, occ, r, k0, k1)) return 0.f;
+  return march<STORE>(V, r, k0, k1, cut);
 }
 
 #ifndef ASC_RAY_MINBLOCKS
@@ -254,34 +256,34 @@ __device__ __forceinline__ float march_any(const DevVolume& V, const uint8_t* oc
 #endif
 __global__ void __launch_bounds__(256, ASC_RAY_MINBLOCKS) k_ray(const SceneDev* __restrict__ sc, Bufs b, int skip)
 {
-  __shared__ int s_tile;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int ox = (warp & 1) * 8 + (lane & 7), oy = (warp >> 1) * 4 + (lane >> 3);
+  // Each warp pulls its own 8 x 4-ray item from the queue: no block barrier,
+  // so a warp with short rays does not wait for the block's longest ray.
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
   const int nv = sc->n_views;
   for (;;) {
-    if (threadIdx.x == 0) s_tile = atomicAdd(&b.C->rnext, 1);
-    __syncthreads();
-    const int tile = s_tile;
-    __syncthreads();
+    __syncwarp();
+    int tile = 0;
+    if (lane == 0) tile = atomicAdd(&b.C->rnext, 1);
+    tile = __shfl_sync(FULL, tile, 0);
     if (tile >= b.C->rtiles) return;
     const int k = find_iv(b.roff, b.C->n_iv, tile);
     const IV& r = b.iv[k];
     const int t = tile - b.roff[k];
-    const int x = (t % r.rtx) * RT + ox, y = (t / r.rtx) * RT + oy;
-    if (x >= r.w || y >= r.h) continue;
+    const int x = (t % r.rtx) * RTX + (lane & 7), y = (t / r.rtx) * RTY + (lane >> 3);
+    const bool valid = x < r.w && y < r.h;
     const BoneDev& B = sc->bones[r.bone];
     const int v = k % nv;
     RaySetup rs;
     float d = 0.f;
-    const bool hit = ray_setup(r.m, r.vp, x, y, df{r.sx[0], r.sx[1]}, df{r.sy[0], r.sy[1]}, B.step[v], B.vol.nx,
-                               B.vol.ny, B.vol.nz, rs);
+    const bool hit = valid && ray_setup(r.m, r.vp, x, y, df{r.sx[0], r.sx[1]}, df{r.sy[0], r.sy[1]}, B.step[v],
+                                        B.vol.nx, B.vol.ny, B.vol.nz, rs);
     {
-      // trilinear samples of this ray (the work figure of the roofline)
-      unsigned cnt = hit ? (unsigned)rs.K : 0u;
-      unsigned mask = __activemask();
-      unsigned tot = __reduce_add_sync(mask, cnt);
-      if ((int)(threadIdx.x & 31) == __ffs(mask) - 1) atomicAdd(&b.C->samples, (unsigned long long)tot);
+      // trilinear samples of this item (the work figure of the roofline)
+      const unsigned tot = __reduce_add_sync(FULL, hit ? (unsigned)rs.K : 0u);
+      if (lane == 0) atomicAdd(&b.C->samples, (unsigned long long)tot);
     }
+    if (!valid) continue;
     if (hit) {
       float cut = B.cutoff_raw[v];
       const uint8_t* occ = skip ? B.occ[v] : nullptr;

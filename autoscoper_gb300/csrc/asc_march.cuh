@@ -6,20 +6,47 @@
 namespace asc {
 
 // --------------------------------------------------------------------------
-// Device volume.  Voxels are stored "x-paired": word (x, y, z) holds voxel
-// x in its low half and voxel min(x+1, nx-1) in its high half, so that one
-// 32-bit load fetches both x taps of a trilinear sample.  The halves are u16
-// integers (ASC_STORE_U16), IEEE half (ASC_STORE_F16) or bfloat16
-// (ASC_STORE_BF16), all holding the stored integer value; `norm` (1/65535
-// or 1/255) turns a raw value into the normalized float that
-// cudaReadModeNormalizedFloat would return.
+// Device volume.  Voxels are stored "x-paired": the word for voxel x holds
+// voxel x in its low half and voxel x+1 in its high half, so that one 32-bit
+// load fetches both x taps of a trilinear sample.  The grid is padded by PAD
+// voxels on every side with copies of the edge voxels, which is
+// clamp-to-edge addressing (cutil_create_tex_obj.h:18-23) built into the
+// layout: the taps of any sample inside the volume box need no per-sample
+// clamping.  The halves are u16 integers (ASC_STORE_U16), IEEE half
+// (ASC_STORE_F16) or bfloat16 (ASC_STORE_BF16), all holding the stored
+// integer value; `norm` (1/65535 or 1/255) turns a raw value into the
+// normalized float that cudaReadModeNormalizedFloat would return.
 // --------------------------------------------------------------------------
+constexpr int PAD = 2;
+
 struct DevVolume {
-  const uint32_t* pairs;  // nz * ny * nx words
-  int nx, ny, nz;
+  const uint32_t* pairs;  // (nz + 2 PAD) slices of (ny + 2 PAD) rows of (nx + 2 PAD) words
+  int nx, ny, nz;         // voxels of the volume itself
+  int px, pxy;            // padded row and slice pitch in words
   int storage;
   float norm;
 };
+
+inline size_t padded_words(int nx, int ny, int nz)
+{
+  return (size_t)(nx + 2 * PAD) * (ny + 2 * PAD) * (nz + 2 * PAD);
+}
+
+// Fills the padded paired layout from stored 16-bit halves v(x, y, z) of an
+// nx x ny x nz volume (host side).
+template <class F>
+inline void pack_pairs(int nx, int ny, int nz, F v, uint32_t* out)
+{
+  const int px = nx + 2 * PAD, py = ny + 2 * PAD, pz = nz + 2 * PAD;
+  auto cl = [](int i, int n) { return i < 0 ? 0 : (i > n - 1 ? n - 1 : i); };
+  for (int zp = 0; zp < pz; ++zp)
+    for (int yp = 0; yp < py; ++yp)
+      for (int xp = 0; xp < px; ++xp) {
+        const int z = cl(zp - PAD, nz), y = cl(yp - PAD, ny);
+        const uint32_t lo = v(cl(xp - PAD, nx), y, z), hi = v(cl(xp - PAD + 1, nx), y, z);
+        out[((size_t)zp * py + yp) * px + xp] = lo | (hi << 16);
+      }
+}
 
 
 template <int STORE>
@@ -241,115 +268,126 @@ __device__ __forceinline__ void coord_base(df C, df dC, float k, int& base_i, fl
   frac = __fadd_rn(__fadd_rn(c.h, -fl), c.l);
 }
 
-// One ray of cuda_volume_render_kernel (RayCaster_kernels.cu:187-195): the K
-// samples from t = far towards near.  Returns the compensated (Kahan) sum of
-// raw samples above cutoff_raw (the caller scales by step * norm /
-// intensity).  With `occ`, runs of samples inside empty cells are stepped
-// over without being read: the same samples contribute, in the same order.
+// Index of the occupancy cell holding the lower tap of a sample at
+// (approximate) texel coordinates X, Y, Z: floor(X / OCC) per axis, clamped.
+__device__ __forceinline__ int occ_cell(float X, float Y, float Z, int bx, int by, int bz, int& cx, int& cy, int& cz)
+{
+  cx = min(max(__float2int_rd(X * (1.0f / OCC)), 0), bx - 1);
+  cy = min(max(__float2int_rd(Y * (1.0f / OCC)), 0), by - 1);
+  cz = min(max(__float2int_rd(Z * (1.0f / OCC)), 0), bz - 1);
+  return (cz * by + cy) * bx + cx;
+}
+
+// Whole samples, after the current one, that stay in cell c along the march
+// (dir = +1: towards near, coordinates move by -d per sample; dir = -1: back
+// towards far).  A 1e-3 voxel margin covers the ~1e-4 error of the FP32
+// coordinates used here.
+__device__ __forceinline__ int cell_run(float X, float Y, float Z, float dX, float dY, float dZ, int cx, int cy, int cz,
+                                        float dir)
+{
+  const float G = 1.0e-3f;
+  const float ex = dX * dir, ey = dY * dir, ez = dZ * dir;  // coordinate decrease per sample
+  float s = 3.0e38f;
+  if (ex > 0.f) s = fminf(s, (X - (float)(OCC * cx) - G) / ex);
+  if (ex < 0.f) s = fminf(s, (X - (float)(OCC * cx + OCC) + G) / ex);
+  if (ey > 0.f) s = fminf(s, (Y - (float)(OCC * cy) - G) / ey);
+  if (ey < 0.f) s = fminf(s, (Y - (float)(OCC * cy + OCC) + G) / ey);
+  if (ez > 0.f) s = fminf(s, (Z - (float)(OCC * cz) - G) / ez);
+  if (ez < 0.f) s = fminf(s, (Z - (float)(OCC * cz + OCC) + G) / ez);
+  return (int)fminf(fmaxf(floorf(s), 0.f), 1.0e7f);
+}
+
+// The first and last samples of a ray whose lower tap lies in an occupied
+// cell; the samples outside [k0, k1] add exactly nothing.  Returns false
+// when none is occupied.
+__device__ __forceinline__ bool occupied_span(const DevVolume& V, const uint8_t* __restrict__ occ, const RaySetup& r,
+                                              int& k0, int& k1)
+{
+  k0 = 0;
+  k1 = r.K - 1;
+  if (!occ || r.K <= 0) return r.K > 0;
+  const int bx = (V.nx + OCC - 1) / OCC, by = (V.ny + OCC - 1) / OCC, bz = (V.nz + OCC - 1) / OCC;
+  const float Xh = r.X.h, Yh = r.Y.h, Zh = r.Z.h, dX = r.dX.h, dY = r.dY.h, dZ = r.dZ.h;
+  int cx, cy, cz;
+  for (;;) {  // from far towards near
+    const float kf = (float)k0;
+    const float X = fmaf(-kf, dX, Xh), Y = fmaf(-kf, dY, Yh), Z = fmaf(-kf, dZ, Zh);
+    if (__ldg(occ + occ_cell(X, Y, Z, bx, by, bz, cx, cy, cz))) break;
+    k0 += cell_run(X, Y, Z, dX, dY, dZ, cx, cy, cz, 1.0f) + 1;
+    if (k0 >= r.K) return false;
+  }
+  for (;;) {  // from near back towards far
+    const float kf = (float)k1;
+    const float X = fmaf(-kf, dX, Xh), Y = fmaf(-kf, dY, Yh), Z = fmaf(-kf, dZ, Zh);
+    if (__ldg(occ + occ_cell(X, Y, Z, bx, by, bz, cx, cy, cz))) break;
+    k1 -= cell_run(X, Y, Z, dX, dY, dZ, cx, cy, cz, -1.0f) + 1;
+    if (k1 < k0) return false;  // cannot happen: k0 is occupied
+  }
+  return true;
+}
+
+// One ray of cuda_volume_render_kernel (RayCaster_kernels.cu:187-195): the
+// samples k0..k1 of the ray (t = far - k).  Returns the compensated (Kahan)
+// sum of raw samples above cutoff_raw (the caller scales by
+// step * norm / intensity).  Sample positions depend on k alone (bases at
+// multiples of REBASE), so the span [k0, k1] chosen by occupied_span changes
+// no bit of the result.
 template <int STORE>
-__device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __restrict__ occ, const RaySetup& r,
-                                       float cutoff_raw)
+__device__ __forceinline__ float march(const DevVolume& V, const RaySetup& r, int k0, int k1, float cutoff_raw)
 {
   const uint32_t* __restrict__ P = V.pairs;
-  const int nx = V.nx, ny = V.ny, nz = V.nz;
-  const int sxy = nx * ny;
-  const int bx = (nx + OCC - 1) / OCC, by = (ny + OCC - 1) / OCC, bz = (nz + OCC - 1) / OCC;
+  const int px = V.px, pxy = V.pxy;
+  const unsigned xmax = (unsigned)(px - 1), ymax = (unsigned)(V.ny + 2 * PAD - 2),
+                 zmax = (unsigned)(V.nz + 2 * PAD - 2);
   const float dXh = r.dX.h, dYh = r.dY.h, dZh = r.dZ.h;
-  // per-sample change of the coordinates, and its reciprocal for the
-  // cell-exit distances (only the sign and a 1e-3 voxel margin matter there)
-  const float iX = dXh != 0.f ? 1.0f / dXh : 0.f, iY = dYh != 0.f ? 1.0f / dYh : 0.f;
-  const float iZ = dZh != 0.f ? 1.0f / dZh : 0.f;
   float acc = 0.f, comp = 0.f;
-  int bix = 0, biy = 0, biz = 0;
-  float bfx = 0.f, bfy = 0.f, bfz = 0.f, fx = 0.f, fy = 0.f, fz = 0.f;
-  int kb = -REBASE;  // index of the current base, a multiple of REBASE
-  float j = 0.f;     // k - kb
-  int kj = 0;        // the k that j belongs to
-  int inside = 0;    // samples from k on known to lie in an occupied cell
-  for (int k = 0; k < r.K;) {
-    if (k - kb >= REBASE) {
-      kb = k & ~(REBASE - 1);
-      const float kf = (float)kb;
-      coord_base(r.X, r.dX, kf, bix, bfx, fx);
-      coord_base(r.Y, r.dY, kf, biy, bfy, fy);
-      coord_base(r.Z, r.dZ, kf, biz, bfz, fz);
-      kj = k - 1;  // force j below
-    }
-    if (kj != k) {  // after a base change or a skip
-      j = (float)(k - kb);
-      kj = k;
-    }
-    // j * (low part of d) stays below 1e-6 voxel for j < REBASE
-    const float FX = fmaf(-j, dXh, fx), FY = fmaf(-j, dYh, fy), FZ = fmaf(-j, dZh, fz);
-    if (occ && inside <= 0) {
-      // the lower tap is floor(X) (or floor(X) - 1 at an integer X, see tap)
-      // and its cell floor(X / OCC); X here is approximate (~1e-5 voxel)
-      const float X = bfx + FX, Y = bfy + FY, Z = bfz + FZ;
-      const int cx = min(max(__float2int_rd(X * (1.0f / OCC)), 0), bx - 1);
-      const int cy = min(max(__float2int_rd(Y * (1.0f / OCC)), 0), by - 1);
-      const int cz = min(max(__float2int_rd(Z * (1.0f / OCC)), 0), bz - 1);
-      // whole samples after this one during which the lower tap stays at
-      // least 1e-3 voxel inside the cell (well above the error of X); a
-      // coordinate moves by -d per sample
-      const float G = 1.0e-3f;
-      float s = 3.0e38f;
-      if (dXh > 0.f) s = fminf(s, (X - (float)(OCC * cx) - G) * iX);
-      if (dXh < 0.f) s = fminf(s, (X - (float)(OCC * cx + OCC) + G) * iX);
-      if (dYh > 0.f) s = fminf(s, (Y - (float)(OCC * cy) - G) * iY);
-      if (dYh < 0.f) s = fminf(s, (Y - (float)(OCC * cy + OCC) + G) * iY);
-      if (dZh > 0.f) s = fminf(s, (Z - (float)(OCC * cz) - G) * iZ);
-      if (dZh < 0.f) s = fminf(s, (Z - (float)(OCC * cz + OCC) + G) * iZ);
-      const int m = (int)fminf(fmaxf(floorf(s), 0.f), 1.0e6f) + 1;  // this sample and the next m - 1
-      if (!__ldg(occ + (cz * by + cy) * bx + cx)) {
-        k += m;  // all of them add nothing
-        continue;
+  for (int kb = k0 & ~(REBASE - 1); kb <= k1; kb += REBASE) {
+    int bix, biy, biz;
+    float bfx, bfy, bfz, fx, fy, fz;
+    const float kbf = (float)kb;
+    coord_base(r.X, r.dX, kbf, bix, bfx, fx);
+    coord_base(r.Y, r.dY, kbf, biy, bfy, fy);
+    coord_base(r.Z, r.dZ, kbf, biz, bfz, fz);
+    // padded indices of the lower taps are base + PAD + tap(fraction)
+    bix += PAD;
+    biy += PAD;
+    biz += PAD;
+    const int ke = min(kb + REBASE - 1, k1);
+    int k = max(kb, k0);
+    float j = (float)(k - kb);
+    for (; k <= ke; ++k, j += 1.0f) {
+      // j * (low part of d) stays below 1e-6 voxel for j < REBASE
+      int ix, iy, iz;
+      float ax, ay, az;
+      tap(fmaf(-j, dXh, fx), ix, ax);
+      tap(fmaf(-j, dYh, fy), iy, ay);
+      tap(fmaf(-j, dZh, fz), iz, az);
+      // inside the box the taps stay in the padded grid; the clamps only keep
+      // degenerate input in bounds
+      const unsigned xp = min((unsigned)(ix + bix), xmax);
+      const unsigned yp = min((unsigned)(iy + biy), ymax);
+      const unsigned zp = min((unsigned)(iz + biz), zmax);
+      const uint32_t* p0 = P + (size_t)zp * pxy + yp * px + xp;
+      const uint32_t w00 = __ldg(p0), w10 = __ldg(p0 + px), w01 = __ldg(p0 + pxy), w11 = __ldg(p0 + pxy + px);
+      float a0, a1, b0, b1, c0, c1, d0, d1;
+      unpack<STORE>(w00, a0, a1);
+      unpack<STORE>(w10, b0, b1);
+      unpack<STORE>(w01, c0, c1);
+      unpack<STORE>(w11, d0, d1);
+      const float e00 = fmaf(ax, a1 - a0, a0);
+      const float e10 = fmaf(ax, b1 - b0, b0);
+      const float e01 = fmaf(ax, c1 - c0, c0);
+      const float e11 = fmaf(ax, d1 - d0, d0);
+      const float f0 = fmaf(ay, e10 - e00, e00);
+      const float f1 = fmaf(ay, e11 - e01, e01);
+      const float s = fmaf(az, f1 - f0, f0);
+      if (s > cutoff_raw) {  // a sample at or below the cutoff leaves the sum untouched
+        const float y = s - comp;
+        const float tt = acc + y;
+        comp = (tt - acc) - y;
+        acc = tt;
       }
-      inside = m;
     }
-    int ix, iy, iz;
-    float ax, ay, az;
-    tap(FX, ix, ax);
-    tap(FY, iy, ay);
-    tap(FZ, iz, az);
-    ix += bix;
-    iy += biy;
-    iz += biz;
-    // clamp-to-edge; below the first texel both taps are texel 0
-    if (ix < 0) { ix = 0; ax = 0.f; }
-    ix = min(ix, nx - 1);
-    int y0 = max(iy, 0), y1 = min(iy + 1, ny - 1);
-    y0 = min(y0, ny - 1);
-    y1 = max(y1, 0);
-    int z0 = max(iz, 0), z1 = min(iz + 1, nz - 1);
-    z0 = min(z0, nz - 1);
-    z1 = max(z1, 0);
-    const int r00 = z0 * sxy + y0 * nx + ix;
-    const int r10 = z0 * sxy + y1 * nx + ix;
-    const int r01 = z1 * sxy + y0 * nx + ix;
-    const int r11 = z1 * sxy + y1 * nx + ix;
-    uint32_t w00 = __ldg(P + r00), w10 = __ldg(P + r10), w01 = __ldg(P + r01), w11 = __ldg(P + r11);
-    float a0, a1, b0, b1, c0, c1, d0, d1;
-    unpack<STORE>(w00, a0, a1);
-    unpack<STORE>(w10, b0, b1);
-    unpack<STORE>(w01, c0, c1);
-    unpack<STORE>(w11, d0, d1);
-    float e00 = fmaf(ax, a1 - a0, a0);
-    float e10 = fmaf(ax, b1 - b0, b0);
-    float e01 = fmaf(ax, c1 - c0, c0);
-    float e11 = fmaf(ax, d1 - d0, d0);
-    float f0 = fmaf(ay, e10 - e00, e00);
-    float f1 = fmaf(ay, e11 - e01, e01);
-    float s = fmaf(az, f1 - f0, f0);
-    if (s > cutoff_raw) {  // a sample at or below the cutoff leaves the sum untouched
-      const float y = s - comp;
-      const float tt = acc + y;
-      comp = (tt - acc) - y;
-      acc = tt;
-    }
-    ++k;
-    ++kj;
-    --inside;
-    j += 1.0f;
   }
   return acc;
 }

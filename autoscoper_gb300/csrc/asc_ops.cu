@@ -67,8 +67,10 @@ __global__ void __launch_bounds__(256) k_raycast(DevVolume V, const uint8_t* __r
   if (x >= w || y >= h) return;
   RaySetup r;
   float d = 0.f;
-  if (ray_setup(a.m, a.vp, x, y, df{a.sx[0], a.sx[1]}, df{a.sy[0], a.sy[1]}, a.step, V.nx, V.ny, V.nz, r))
-    d = march<STORE>(V, occ, r, a.cutoff_raw) * a.scale;
+  if (ray_setup(a.m, a.vp, x, y, df{a.sx[0], a.sx[1]}, df{a.sy[0], a.sy[1]}, a.step, V.nx, V.ny, V.nz, r)) {
+    int k0, k1;
+    if (occupied_span(V, occ, r, k0, k1)) d = march<STORE>(V, r, k0, k1, a.cutoff_raw) * a.scale;
+  }
   out[(size_t)y * w + x] = fminf(fmaxf(d, 0.f), 1.f);
 }
 
@@ -404,7 +406,7 @@ __global__ void k_occupancy(DevVolume V, float cutoff_raw, uint8_t* __restrict__
     for (int y = max(cy * OCC - 1, 0); y < min(cy * OCC + OCC + 1, V.ny); ++y)
       for (int x = max(cx * OCC - 1, 0); x < min(cx * OCC + OCC + 1, V.nx); ++x) {
         float lo, hi;
-        unpack<STORE>(V.pairs[(size_t)z * V.nx * V.ny + (size_t)y * V.nx + x], lo, hi);
+        unpack<STORE>(V.pairs[(size_t)(z + PAD) * V.pxy + (size_t)(y + PAD) * V.px + (x + PAD)], lo, hi);
         mx = fmaxf(mx, lo);
       }
   occ[c] = mx > cutoff_raw ? 1 : 0;
@@ -719,22 +721,22 @@ ASC_API int asc_volume_create(const void* data, int W, int H, int D, int bps, co
   v->inv_trans[1] = -((H - mx[1] - 1) / (float)dims[1]);
   v->inv_trans[2] = mn[2] / (float)dims[2];
   v->bps = bps;
-  // x-paired words (see DevVolume)
-  size_t nvox = (size_t)dims[0] * dims[1] * dims[2];
-  std::vector<uint32_t> pairs(nvox);
-  for (size_t r = 0; r < nvox / dims[0]; ++r)
-    for (int x = 0; x < dims[0]; ++x) {
-      unsigned lo = vals[r * dims[0] + x], hi = vals[r * dims[0] + std::min(x + 1, dims[0] - 1)];
-      pairs[r * dims[0] + x] = (uint32_t)to_store(lo, storage) | ((uint32_t)to_store(hi, storage) << 16);
-    }
-  cudaError_t e = cudaMalloc(&v->pairs, nvox * sizeof(uint32_t));
-  if (e == cudaSuccess) e = cudaMemcpy(v->pairs, pairs.data(), nvox * sizeof(uint32_t), cudaMemcpyHostToDevice);
+  // x-paired words on the padded grid (see DevVolume)
+  const size_t nwords = padded_words(dims[0], dims[1], dims[2]);
+  std::vector<uint32_t> pairs(nwords);
+  const int dx = dims[0], dxy = dims[0] * dims[1];
+  pack_pairs(dims[0], dims[1], dims[2],
+             [&](int x, int y, int z) { return (uint32_t)to_store(vals[(size_t)z * dxy + (size_t)y * dx + x], storage); },
+             pairs.data());
+  cudaError_t e = cudaMalloc(&v->pairs, nwords * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemcpy(v->pairs, pairs.data(), nwords * sizeof(uint32_t), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     if (v->pairs) cudaFree(v->pairs);
     delete v;
     return cuda_status(e);
   }
-  v->dev = DevVolume{v->pairs, dims[0], dims[1], dims[2], storage, 1.0f / norm};
+  const int px = dims[0] + 2 * PAD, pxy = px * (dims[1] + 2 * PAD);
+  v->dev = DevVolume{v->pairs, dims[0], dims[1], dims[2], px, pxy, storage, 1.0f / norm};
   *out = (asc_volume)v;
   return ASC_OK;
 }

@@ -23,14 +23,13 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
                           int* nsamples)
 {
   if (storage != ASC_STORE_U16 && storage != ASC_STORE_BF16) return -1;
-  std::vector<uint32_t> pairs((size_t)nx * ny * nz);
-  for (size_t r = 0; r < (size_t)ny * nz; ++r)
-    for (int x = 0; x < nx; ++x) {
-      unsigned lo = vol[r * nx + x], hi = vol[r * nx + std::min(x + 1, nx - 1)];
-      if (storage == ASC_STORE_BF16) { lo = to_bf16(lo); hi = to_bf16(hi); }
-      pairs[r * nx + x] = lo | (hi << 16);
-    }
-  DevVolume V{pairs.data(), nx, ny, nz, storage, 1.0f / 65535.0f};
+  std::vector<uint32_t> pairs(padded_words(nx, ny, nz));
+  pack_pairs(nx, ny, nz, [&](int x, int y, int z) {
+    unsigned v = vol[((size_t)z * ny + y) * nx + x];
+    return (uint32_t)(storage == ASC_STORE_BF16 ? to_bf16(v) : v);
+  }, pairs.data());
+  const int px = nx + 2 * PAD, pxy = px * (ny + 2 * PAD);
+  DevVolume V{pairs.data(), nx, ny, nz, px, pxy, storage, 1.0f / 65535.0f};
   const float cut = cutoff / V.norm;
   // occupancy as k_occupancy builds it
   const int bx = (nx + OCC - 1) / OCC, by = (ny + OCC - 1) / OCC, bz = (nz + OCC - 1) / OCC;
@@ -43,7 +42,7 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
           for (int y = std::max(cy * OCC - 1, 0); y < std::min(cy * OCC + OCC + 1, ny); ++y)
             for (int x = std::max(cx * OCC - 1, 0); x < std::min(cx * OCC + OCC + 1, nx); ++x) {
               float lo, hi;
-              uint32_t wd = pairs[(size_t)z * nx * ny + (size_t)y * nx + x];
+              uint32_t wd = pairs[(size_t)(z + PAD) * pxy + (size_t)(y + PAD) * px + (x + PAD)];
               if (storage == ASC_STORE_BF16) unpack<ASC_STORE_BF16>(wd, lo, hi);
               else unpack<ASC_STORE_U16>(wd, lo, hi);
               mx = std::max(mx, lo);
@@ -60,7 +59,10 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
       df_split((double)vp[3] / (double)h, sy.h, sy.l);
       if (ray_setup(m, vp, x, y, sx, sy, step, nx, ny, nz, r)) {
         const uint8_t* o = skip ? occ.data() : nullptr;
-        float acc = storage == ASC_STORE_BF16 ? march<ASC_STORE_BF16>(V, o, r, cut) : march<ASC_STORE_U16>(V, o, r, cut);
+        int k0, k1;
+        float acc = 0.f;
+        if (occupied_span(V, o, r, k0, k1))
+          acc = storage == ASC_STORE_BF16 ? march<ASC_STORE_BF16>(V, r, k0, k1, cut) : march<ASC_STORE_U16>(V, r, k0, k1, cut);
         d = acc * (step * V.norm / intensity);
         n = r.K;
       }
