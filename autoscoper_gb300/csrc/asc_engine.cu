@@ -8,7 +8,7 @@
 //                            (item, view) crop, with prefix sums;
 //   k_ray         persistent: 16x16-ray tiles pulled from an atomic queue,
 //                            DRRs written to a packed buffer;
-//   k_view        persistent: 32x32 output tiles pulled from a queue; each
+//   k_view        persistent: 64x64 output tiles pulled from a queue; each
 //                            stages DRR and radiograph regions with the chain's
 //                            halo in shared memory, runs both filter chains,
 //                            the masks and the NCC moments; the last tile of a
@@ -36,8 +36,18 @@ namespace {
 constexpr int MAX_VIEWS = 4;
 constexpr int MAX_BONES = 16;
 constexpr int MAX_FILTERS = 8;
-constexpr int VT = 32;   // k_view output tile edge
-constexpr int RTX = 8, RTY = 4;  // k_ray work item: one warp, 8 x 4 rays
+#ifndef ASC_VT
+#define ASC_VT 64
+#endif
+#ifndef ASC_VIEW_MINBLOCKS
+#define ASC_VIEW_MINBLOCKS 2
+#endif
+constexpr int VT = ASC_VT;   // k_view output tile edge
+constexpr int VNT = 256;     // k_view threads per block
+constexpr int RTX = 16, RTY = 16;  // k_ray work item: one block, 16 x 16 rays
+constexpr int NRAY = RTX * RTY;    // k_ray threads per block, one ray each
+constexpr int NBW = 8;             // march blocks per ray per k_ray pass
+constexpr int SEGCAP = 1024;       // march segments per k_ray pass
 
 struct FilterDev {
   int kind, K, R;
@@ -87,6 +97,7 @@ struct Counters {
   int error;
   int pad;
   unsigned long long samples, pixels;
+  unsigned long long marched, slots;  // marched samples, 32 x warp-max span
 };
 
 struct Bufs {
@@ -229,6 +240,8 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
     b.C->fnext = 0;
     b.C->error = s_err;
     b.C->samples = 0;
+    b.C->marched = 0;
+    b.C->slots = 0;
     b.C->pixels = (unsigned long long)(sp[threadIdx.x]);
   }
   __syncthreads();
@@ -243,68 +256,175 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
 }
 
 // ---------------------------------------------------------------- k_ray
-template <int STORE>
-__device__ __forceinline__ float march_any(const DevVolume& V, const uint8_t* occ, const RaySetup& r, float cut)
-{
-  int k0, k1;
-  if (!occupied_span(V, occ, r, k0, k1)) return 0.f;
-  return march<STORE>(V, r, k0, k1, cut);
-}
-
 #ifndef ASC_RAY_MINBLOCKS
 #define ASC_RAY_MINBLOCKS 4  // 4 x 256 threads resident per SM (<= 64 registers)
 #endif
-__global__ void __launch_bounds__(256, ASC_RAY_MINBLOCKS) k_ray(const SceneDev* __restrict__ sc, Bufs b, int skip)
+
+// Rays of one 16 x 16 tile of one (item, view) crop per block.  Each ray's
+// march is cut into segments: the REBASE-sample march blocks that hold
+// occupied samples, each trimmed to its occupied extent (block_extent).  The
+// block's segments are sorted by length (counting sort, longest first) and
+// marched 32 at a time by whichever warp is free, so the lanes of a warp
+// march segments of nearly equal length whatever the rays' lengths; each
+// ray then adds its blocks' sums in order (add_block), as march() does for
+// a single ray.  A ray with more than NBW blocks, or a tile with more than
+// SEGCAP segments, takes further passes.
+template <int STORE>
+__device__ __forceinline__ void march_segments(const DevVolume& V, const float4 (*rec)[NRAY], const int* b0,
+                                               const unsigned* ord, float2* part, int nseg, int* grab, float cut,
+                                               unsigned long long& marched, unsigned long long& slots)
 {
-  // Each warp pulls its own 8 x 4-ray item from the queue: no block barrier,
-  // so a warp with short rays does not wait for the block's longest ray.
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  const int nv = sc->n_views;
   for (;;) {
-    __syncwarp();
-    int tile = 0;
-    if (lane == 0) tile = atomicAdd(&b.C->rnext, 1);
-    tile = __shfl_sync(FULL, tile, 0);
-    if (tile >= b.C->rtiles) return;
+    int g = 0;
+    if (lane == 0) g = atomicAdd(grab, 32);
+    g = __shfl_sync(FULL, g, 0);
+    if (g >= nseg) return;
+    int len = 0;
+    if (g + lane < nseg) {
+      const unsigned d = ord[g + lane];
+      const int slot = d & 2047u, js = (d >> 11) & 63u, je = (d >> 17) & 63u;
+      const int ray = slot / NBW;
+      RaySetup r;
+      const float4 q0 = rec[0][ray], q1 = rec[1][ray], q2 = rec[2][ray];
+      r.X = df{q0.x, q0.y};
+      r.Y = df{q0.z, q0.w};
+      r.Z = df{q1.x, q1.y};
+      r.dX = df{q1.z, q1.w};
+      r.dY = df{q2.x, q2.y};
+      r.dZ = df{q2.z, q2.w};
+      const int kb = (b0[ray] + slot % NBW) * REBASE;
+      part[slot] = march_block<STORE>(V, r, kb, js, je, cut);
+      len = je - js + 1;
+    }
+    const unsigned tot = __reduce_add_sync(FULL, (unsigned)len), mx = __reduce_max_sync(FULL, (unsigned)len);
+    marched += tot;
+    slots += 32ull * mx;
+  }
+}
+
+__global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev* __restrict__ sc, Bufs b, int skip)
+{
+  static_assert(REBASE == 64 && NRAY * NBW <= 2048, "segment fields: 11-bit slot, 6-bit offsets");
+  __shared__ float4 s_rec[3][NRAY];      // per ray: X, Y, Z, dX, dY, dZ as double-floats
+  __shared__ float2 s_part[NRAY * NBW];  // per ray and march block: (sum, compensation)
+  __shared__ unsigned s_seg[SEGCAP];     // segments: slot | js << 11 | je << 17
+  __shared__ unsigned s_ord[SEGCAP];     // the same, longest first
+  __shared__ int s_b0[NRAY];             // first march block of each ray in this pass
+  __shared__ int s_cnt[REBASE];          // segments per length - 1, then placement cursors
+  __shared__ int s_tile, s_nseg, s_grab;
+  const unsigned FULL = 0xffffffffu;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int nv = sc->n_views;
+  unsigned long long marched = 0, slots = 0;
+  for (;;) {
+    if (tid == 0) s_tile = atomicAdd(&b.C->rnext, 1);
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= b.C->rtiles) break;
     const int k = find_iv(b.roff, b.C->n_iv, tile);
     const IV& r = b.iv[k];
     const int t = tile - b.roff[k];
-    const int x = (t % r.rtx) * RTX + (lane & 7), y = (t / r.rtx) * RTY + (lane >> 3);
+    const int x = (t % r.rtx) * RTX + (tid % RTX), y = (t / r.rtx) * RTY + (tid / RTX);
     const bool valid = x < r.w && y < r.h;
     const BoneDev& B = sc->bones[r.bone];
     const int v = k % nv;
-    RaySetup rs;
-    float d = 0.f;
+    const float cut = B.cutoff_raw[v];
+    const uint8_t* occ = skip ? B.occ[v] : nullptr;
+    RaySetup rs{};
     const bool hit = valid && ray_setup(r.m, r.vp, x, y, df{r.sx[0], r.sx[1]}, df{r.sy[0], r.sy[1]}, B.step[v],
                                         B.vol.nx, B.vol.ny, B.vol.nz, rs);
     {
-      // trilinear samples of this item (the work figure of the roofline)
+      // trilinear samples of the reference's march (the work figure of the roofline)
       const unsigned tot = __reduce_add_sync(FULL, hit ? (unsigned)rs.K : 0u);
       if (lane == 0) atomicAdd(&b.C->samples, (unsigned long long)tot);
     }
-    if (!valid) continue;
-    if (hit) {
-      float cut = B.cutoff_raw[v];
-      const uint8_t* occ = skip ? B.occ[v] : nullptr;
-      float acc;
-      if (B.vol.storage == ASC_STORE_BF16)
-        acc = march_any<ASC_STORE_BF16>(B.vol, occ, rs, cut);
-      else if (B.vol.storage == ASC_STORE_F16)
-        acc = march_any<ASC_STORE_F16>(B.vol, occ, rs, cut);
-      else
-        acc = march_any<ASC_STORE_U16>(B.vol, occ, rs, cut);
-      d = acc * B.scale[v];
+    int kw = 1, kend = 0;  // samples still to walk: [kw, kend]
+    if (hit && occupied_span(B.vol, occ, rs, kw, kend)) {
+      s_rec[0][tid] = make_float4(rs.X.h, rs.X.l, rs.Y.h, rs.Y.l);
+      s_rec[1][tid] = make_float4(rs.Z.h, rs.Z.l, rs.dX.h, rs.dX.l);
+      s_rec[2][tid] = make_float4(rs.dY.h, rs.dY.l, rs.dZ.h, rs.dZ.l);
+    } else {
+      kw = 1;
+      kend = 0;
     }
-    b.drr[r.pix + (long long)y * r.w + x] = fminf(fmaxf(d, 0.f), 1.f);
+    const CellWalk cw = cell_walk(B.vol, rs);
+    df total{0.f, 0.f};
+    for (;;) {
+      if (tid < REBASE) s_cnt[tid] = 0;
+      if (tid == 0) {
+        s_nseg = 0;
+        s_grab = 0;
+      }
+      __syncthreads();
+      // ---- walk: this pass's segments of this ray
+      unsigned mask = 0;
+      const int b0 = kw / REBASE;
+      s_b0[tid] = b0;
+      while (kw <= kend) {
+        const int kb = (kw / REBASE) * REBASE, i = kw / REBASE - b0;
+        if (i >= NBW) break;
+        int first, last;
+        if (block_extent(cw, occ, kw, min(kb + REBASE - 1, kend), first, last)) {
+          const int at = atomicAdd(&s_nseg, 1);
+          if (at >= SEGCAP) break;  // resume at this block in the next pass
+          s_seg[at] = (unsigned)(tid * NBW + i) | (unsigned)(first - kb) << 11 | (unsigned)(last - kb) << 17;
+          atomicAdd(&s_cnt[last - first], 1);
+          mask |= 1u << i;
+        }
+        kw = kb + REBASE;
+      }
+      __syncthreads();
+      const int nseg = min(s_nseg, SEGCAP);
+      // ---- counting sort by length, longest first
+      if (tid < 32) {
+        const int c0 = s_cnt[REBASE - 1 - 2 * lane], c1 = s_cnt[REBASE - 2 - 2 * lane];
+        int incl = c0 + c1;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int u = __shfl_up_sync(FULL, incl, o);
+          if (lane >= o) incl += u;
+        }
+        const int excl = incl - c0 - c1;
+        s_cnt[REBASE - 1 - 2 * lane] = excl;
+        s_cnt[REBASE - 2 - 2 * lane] = excl + c0;
+      }
+      __syncthreads();
+      for (int i = tid; i < nseg; i += NRAY) {
+        const unsigned d = s_seg[i];
+        const int len1 = (int)((d >> 17) & 63u) - (int)((d >> 11) & 63u);
+        s_ord[atomicAdd(&s_cnt[len1], 1)] = d;
+      }
+      __syncthreads();
+      // ---- march the segments, 32 at a time per warp
+      if (B.vol.storage == ASC_STORE_BF16)
+        march_segments<ASC_STORE_BF16>(B.vol, s_rec, s_b0, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
+      else if (B.vol.storage == ASC_STORE_F16)
+        march_segments<ASC_STORE_F16>(B.vol, s_rec, s_b0, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
+      else
+        march_segments<ASC_STORE_U16>(B.vol, s_rec, s_b0, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
+      __syncthreads();
+      // ---- this ray's blocks, in order
+      for (int i = 0; i < NBW; ++i)
+        if (mask >> i & 1u) add_block(total, s_part[tid * NBW + i]);
+      if (!__syncthreads_or(kw <= kend)) break;
+    }
+    if (valid) b.drr[r.pix + (long long)y * r.w + x] = fminf(fmaxf((total.h + total.l) * B.scale[v], 0.f), 1.f);
+  }
+  if (lane == 0 && slots) {
+    atomicAdd(&b.C->marched, marched);
+    atomicAdd(&b.C->slots, slots);
   }
 }
 
 // ---------------------------------------------------------------- k_view
 // Region coordinates: buffer index (ry, rx) <-> image (y0 + ry, x0 + rx) with
 // x0 = tile x - E_h, where E_h = (E - VT) / 2 is the largest chain halo.
+// `in` is set when the whole E x E region lies inside the image: the stages
+// then skip every bounds test.
 struct Region {
   int x0, y0, E, w, h;
+  bool in;
 };
 
 __device__ __forceinline__ bool inside(const Region& g, int ry, int rx)
@@ -313,73 +433,122 @@ __device__ __forceinline__ bool inside(const Region& g, int ry, int rx)
   return x >= 0 && x < g.w && y >= 0 && y < g.h;
 }
 
+// Calls f(ry, rx) for every position of the band [y0, y1) x [x0, x1), the
+// positions dealt to the block's threads in row-major order (consecutive
+// threads take consecutive columns, wrapping to the next row), so no lane
+// idles on bands narrower or wider than a warp.
+template <class F>
+__device__ __forceinline__ void for_band(int y0, int y1, int x0, int x1, F&& f)
+{
+  const int bw = x1 - x0, n = bw * (y1 - y0);
+  if (bw <= 0 || n <= 0) return;
+  const int dq = VNT / bw, dr = VNT - dq * bw;
+  int ry = (int)threadIdx.x / bw;
+  int rx = (int)threadIdx.x - ry * bw;
+  ry += y0;
+  for (int i = threadIdx.x; i < n; i += VNT) {
+    f(ry, x0 + rx);
+    rx += dr;
+    ry += dq;
+    if (rx >= bw) {
+      rx -= bw;
+      ++ry;
+    }
+  }
+}
+
+// axy^e1 * v^e2 of ContrastFilter_kernels.cu (two powf there) as one exp2 of
+// the summed logarithms; axy > 0.01 here.  v^0 is 1 for every v, as powf's.
+__device__ __forceinline__ float contrast_pow(float axy, float v, float e1, float e2)
+{
+  float l = e1 * log2f(axy);
+  if (e2 != 0.f) l = fmaf(e2, log2f(v), l);
+  return exp2f(l);
+}
+
 // Applies one filter from `in` to `out` over the square band
 // [lo, hi) x [lo, hi) of region coordinates; positions outside the image get
 // 0.  `tmp` holds the horizontal pass of a Gaussian/Sharpen blur, `wsh` its
-// 1-D weights.  Threads map to (row, column) as 8 x 32.
+// 1-D weights.  IN: the region lies inside the image.
+template <bool IN>
 __device__ void apply_stage(const FilterDev& f, const float* in, float* out, float* tmp, float* wsh, const Region& g,
                             int lo, int hi)
 {
   const int E = g.E;
-  const int ty = threadIdx.x >> 5, tx = threadIdx.x & 31;
   const int kind = f.kind, K = f.K, R = f.R;
   const float p0 = f.p0, p1 = f.p1, p2 = f.p2;
   if (kind == 3 || kind == 4) {
     if (threadIdx.x < K) wsh[threadIdx.x] = f.g[threadIdx.x];
     __syncthreads();
     // horizontal pass over rows [lo - R, hi + R)
-    for (int ry = lo - R + ty; ry < hi + R; ry += 8)
-      for (int rx = lo + tx; rx < hi; rx += 32) {
-        const float* p = in + ry * E + rx - R;
-        float s = 0.f;
-        for (int k = 0; k < K; ++k) s = fmaf(wsh[k], p[k], s);
-        tmp[ry * E + rx] = s;
-      }
+    for_band(lo - R, hi + R, lo, hi, [&](int ry, int rx) {
+      const float* p = in + ry * E + rx - R;
+      float s = 0.f;
+      for (int k = 0; k < K; ++k) s = fmaf(wsh[k], p[k], s);
+      tmp[ry * E + rx] = s;
+    });
     __syncthreads();
-    for (int ry = lo + ty; ry < hi; ry += 8)
-      for (int rx = lo + tx; rx < hi; rx += 32) {
-        float r = 0.f;
-        if (inside(g, ry, rx)) {
-          const float* p = tmp + (ry - R) * E + rx;
-          float blur = 0.f;
-          for (int k = 0; k < K; ++k) blur = fmaf(wsh[k], p[k * E], blur);
-          if (kind == 3) {
-            r = fminf(fmaxf(blur, 0.f), 1.f);
-          } else {
-            float v = in[ry * E + rx];
-            r = fabsf(v - blur) > p2 ? fminf(fmaxf(v + p1 * (v - blur), 0.f), 1.f) : v;
-          }
+    for_band(lo, hi, lo, hi, [&](int ry, int rx) {
+      float r = 0.f;
+      if (IN || inside(g, ry, rx)) {
+        const float* p = tmp + (ry - R) * E + rx;
+        float blur = 0.f;
+        for (int k = 0; k < K; ++k) blur = fmaf(wsh[k], p[k * E], blur);
+        if (kind == 3) {
+          r = fminf(fmaxf(blur, 0.f), 1.f);
+        } else {
+          float v = in[ry * E + rx];
+          r = fabsf(v - blur) > p2 ? fminf(fmaxf(v + p1 * (v - blur), 0.f), 1.f) : v;
         }
-        out[ry * E + rx] = r;
       }
+      out[ry * E + rx] = r;
+    });
   } else if (kind == 1) {
-    for (int ry = lo + ty; ry < hi; ry += 8)
-      for (int rx = lo + tx; rx < hi; rx += 32) {
-        float r = 0.f;
-        if (inside(g, ry, rx)) {
+    for_band(lo, hi, lo, hi, [&](int ry, int rx) {
+      float r = 0.f;
+      if (IN || inside(g, ry, rx)) {
+        int xm = -1, xp = 1, ym = -E, yp = E;
+        if (!IN) {
           int x = g.x0 + rx, y = g.y0 + ry;
-          int xm = x > 0 ? -1 : 0, xp = x < g.w - 1 ? 1 : 0, ym = y > 0 ? -E : 0, yp = y < g.h - 1 ? E : 0;
-          const float* c = in + ry * E + rx;
-          float p00 = c[ym + xm], p01 = c[ym], p02 = c[ym + xp];
-          float p10 = c[xm], p11 = c[0], p12 = c[xp];
-          float p20 = c[yp + xm], p21 = c[yp], p22 = c[yp + xp];
-          float horz = p02 + 2 * p12 + p22 - p00 - 2 * p10 - p20;
-          float vert = p00 + 2 * p01 + p02 - p20 - 2 * p21 - p22;
-          float grad = sqrtf(horz * horz + vert * vert);
-          float s = p1 < 0.5f ? p0 * grad + 2.0f * p1 * p11 : 2.0f * (1.0f - p1) * p0 * grad + p11;
-          r = fminf(fmaxf(s, 0.f), 1.f);
+          xm = x > 0 ? -1 : 0;
+          xp = x < g.w - 1 ? 1 : 0;
+          ym = y > 0 ? -E : 0;
+          yp = y < g.h - 1 ? E : 0;
         }
-        out[ry * E + rx] = r;
+        const float* c = in + ry * E + rx;
+        float p00 = c[ym + xm], p01 = c[ym], p02 = c[ym + xp];
+        float p10 = c[xm], p11 = c[0], p12 = c[xp];
+        float p20 = c[yp + xm], p21 = c[yp], p22 = c[yp + xp];
+        float horz = p02 + 2 * p12 + p22 - p00 - 2 * p10 - p20;
+        float vert = p00 + 2 * p01 + p02 - p20 - 2 * p21 - p22;
+        float grad = sqrtf(horz * horz + vert * vert);
+        float s = p1 < 0.5f ? p0 * grad + 2.0f * p1 * p11 : 2.0f * (1.0f - p1) * p0 * grad + p11;
+        r = fminf(fmaxf(s, 0.f), 1.f);
       }
+      out[ry * E + rx] = r;
+    });
   } else if (kind == 0) {
-    const int size = K;
-    for (int ry = lo + ty; ry < hi; ry += 8)
-      for (int rx = lo + tx; rx < hi; rx += 32) {
+    const int size = K, h0 = size / 2, h1 = (size + 1) / 2;
+    const float e1 = p0 - p1, e2 = p1;
+    if (IN) {
+      // every window is whole: size * size taps (the count the reference
+      // accumulates by adding 1.0f per tap is exact)
+      const float cnt = (float)(size * size);
+      for_band(lo, hi, lo, hi, [&](int ry, int rx) {
+        const float* c = in + (ry - h0) * E + rx - h0;
+        float s = 0.f;
+        for (int a = 0; a < size; ++a, c += E)
+          for (int q = 0; q < size; ++q) s += c[q];
+        float axy = s / cnt, v = in[ry * E + rx];
+        out[ry * E + rx] = axy > 0.01f ? contrast_pow(axy, v, e1, e2) : 0.0f;
+      });
+    } else {
+      for_band(lo, hi, lo, hi, [&](int ry, int rx) {
         float r = 0.f;
         if (inside(g, ry, rx)) {
           int x = g.x0 + rx, y = g.y0 + ry;
-          int i0 = max(y - size / 2, 0), i1 = min(y + (size + 1) / 2, g.h);
-          int j0 = max(x - size / 2, 0), j1 = min(x + (size + 1) / 2, g.w);
+          int i0 = max(y - h0, 0), i1 = min(y + h1, g.h);
+          int j0 = max(x - h0, 0), j1 = min(x + h1, g.w);
           float cnt = 0.f, s = 0.f;
           for (int yy = i0; yy < i1; ++yy)
             for (int xx = j0; xx < j1; ++xx) {
@@ -387,10 +556,11 @@ __device__ void apply_stage(const FilterDev& f, const float* in, float* out, flo
               s += in[(yy - g.y0) * E + (xx - g.x0)];
             }
           float axy = s / cnt, v = in[ry * E + rx];
-          r = axy > 0.01f ? powf(axy, p0 - p1) * powf(v, p1) : 0.0f;
+          r = axy > 0.01f ? contrast_pow(axy, v, e1, e2) : 0.0f;
         }
         out[ry * E + rx] = r;
-      }
+      });
+    }
   }
   __syncthreads();
 }
@@ -404,7 +574,10 @@ __device__ int run_chain(const FilterDev* fl, int nf, int H, float* bufs[3], flo
     const FilterDev& f = fl[s];
     int nh = halo - f.R;
     int nxt = cur == 0 ? 1 : 0;
-    apply_stage(f, bufs[cur], bufs[nxt], bufs[2], wsh, g, eh - nh, eh + VT + nh);
+    if (g.in)
+      apply_stage<true>(f, bufs[cur], bufs[nxt], bufs[2], wsh, g, eh - nh, eh + VT + nh);
+    else
+      apply_stage<false>(f, bufs[cur], bufs[nxt], bufs[2], wsh, g, eh - nh, eh + VT + nh);
     cur = nxt;
     halo = nh;
   }
@@ -436,18 +609,17 @@ __device__ void bsum(float (&v)[N], float* red)
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(256, 3) k_view(const SceneDev* __restrict__ sc, Bufs b, double* __restrict__ cost,
-                                              double* __restrict__ view_cost_out)
+__global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
+    k_view(const SceneDev* __restrict__ sc, Bufs b, double* __restrict__ cost, double* __restrict__ view_cost_out)
 {
   extern __shared__ float smem[];
   __shared__ int s_tile;
   __shared__ bool s_last;
   __shared__ float red[8 * 6];
   __shared__ float wsh[32];
-  const int ty = threadIdx.x >> 5, tx = threadIdx.x & 31;
   const int E = sc->E, eh = (E - VT) / 2;
   float* bufs[3] = {smem, smem + E * E, smem + 2 * E * E};
-  float* fdrr = smem + 3 * E * E;        // VT x VT final DRR
+  float* fdrr = smem + 3 * E * E;        // VT x VT final DRR, then f = DRR * mask
   Moments* msh = (Moments*)smem;          // reused by the merge
   const int nv = sc->n_views;
   for (;;) {
@@ -462,47 +634,48 @@ __global__ void __launch_bounds__(256, 3) k_view(const SceneDev* __restrict__ sc
     const int tx0 = (t % r.ftx) * VT, ty0 = (t / r.ftx) * VT;
     const int v = k % nv;
     const ViewDev& V = sc->views[v];
-    Region g{tx0 - eh, ty0 - eh, E, r.w, r.h};
+    const int rx0 = tx0 - eh, ry0 = ty0 - eh;
+    const Region g{rx0, ry0, E, r.w, r.h, rx0 >= 0 && ry0 >= 0 && rx0 + E <= r.w && ry0 + E <= r.h};
     const float* drr = b.drr + r.pix;
     // ---- DRR chain
     {
       const int lo = eh - V.h_drr, hi = eh + VT + V.h_drr;
-      for (int ry = lo + ty; ry < hi; ry += 8)
-        for (int rx = lo + tx; rx < hi; rx += 32)
-          bufs[0][ry * E + rx] = inside(g, ry, rx) ? __ldg(drr + (long long)(g.y0 + ry) * r.w + g.x0 + rx) : 0.f;
+      for_band(lo, hi, lo, hi, [&](int ry, int rx) {
+        bufs[0][ry * E + rx] =
+            (g.in || inside(g, ry, rx)) ? __ldg(drr + (long long)(g.y0 + ry) * r.w + g.x0 + rx) : 0.f;
+      });
       __syncthreads();
       int res = run_chain(V.fdrr, V.n_drr, V.h_drr, bufs, wsh, g, eh);
-      for (int i = threadIdx.x; i < VT * VT; i += blockDim.x)
-        fdrr[i] = bufs[res][(eh + i / VT) * E + eh + i % VT];
+      for (int i = threadIdx.x; i < VT * VT; i += VNT) fdrr[i] = bufs[res][(eh + i / VT) * E + eh + i % VT];
       __syncthreads();
     }
     // ---- radiograph crop and its chain
     int rres;
     {
       const int lo = eh - V.h_rad, hi = eh + VT + V.h_rad;
-      for (int ry = lo + ty; ry < hi; ry += 8)
-        for (int rx = lo + tx; rx < hi; rx += 32) {
-          float val = 0.f, s, tt;
-          if (inside(g, ry, rx) && image_coords(V.ipf, r.vp, g.x0 + rx, g.y0 + ry, r.w, r.h, s, tt))
-            val = 1.0f - bilinear(V.rad, V.rad_bps, V.rad_w, V.rad_h, s, tt);
-          bufs[0][ry * E + rx] = val;
-        }
+      for_band(lo, hi, lo, hi, [&](int ry, int rx) {
+        float val = 0.f, s, tt;
+        if ((g.in || inside(g, ry, rx)) && image_coords(V.ipf, r.vp, g.x0 + rx, g.y0 + ry, r.w, r.h, s, tt))
+          val = 1.0f - bilinear(V.rad, V.rad_bps, V.rad_w, V.rad_h, s, tt);
+        bufs[0][ry * E + rx] = val;
+      });
       __syncthreads();
       rres = run_chain(V.frad, V.n_rad, V.h_rad, bufs, wsh, g, eh);
     }
-    // ---- masks and moments (Tracker.cpp:744-770)
+    // ---- masks and moments (Tracker.cpp:744-770), two passes over the
+    // tile: f = DRR * mask over fdrr, g = rad * mask over the chain result,
+    // the m > 0.5 flags in the free blur buffer
     const unsigned n = (unsigned)r.w * (unsigned)r.h;
     const bool tree = sc->coverage == ASC_SUM_TREE;
-    float fv[4], gv[4];
-    unsigned flags = 0;
+    float* gres = bufs[rres];
+    float* flag = bufs[2];
     float s[6] = {0, 0, 0, 0, 0, 0};
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      int i = threadIdx.x + q * 256;
-      int ly = i / VT, lx = i % VT, x = tx0 + lx, y = ty0 + ly;
-      fv[q] = gv[q] = 0.f;
+    for (int i = threadIdx.x; i < VT * VT; i += VNT) {
+      const int ly = i / VT, lx = i % VT, x = tx0 + lx, y = ty0 + ly;
+      const int gi = (eh + ly) * E + eh + lx;
+      float f = 0.f, gm = 0.f, fl = 0.f;
       if (x < r.w && y < r.h && (!tree || tree_keep((unsigned)(y * r.w + x), n))) {
-        float d = fdrr[i], gg = bufs[rres][(eh + ly) * E + eh + lx];
+        float d = fdrr[i], gg = gres[gi];
         float bg = 1.0f;
         if (V.bg && V.bg_thr >= 0.f) {
           float ss, tt;
@@ -511,28 +684,29 @@ __global__ void __launch_bounds__(256, 3) k_view(const SceneDev* __restrict__ sc
                  : 0.0f;
         }
         float m = bg * (d != 0.0f ? 1.0f : 0.0f);
-        float f = d * m, gm = gg * m;
-        fv[q] = f;
-        gv[q] = gm;
-        flags |= 1u << q;
+        f = d * m;
+        gm = gg * m;
         s[0] += m;
         s[1] += f;
         s[2] += gm;
         if (m > 0.5f) {
-          flags |= 1u << (8 + q);
+          fl = 1.f;
           s[3] += 1.f;
           s[4] += f;
           s[5] += gm;
         }
       }
+      fdrr[i] = f;
+      gres[gi] = gm;
+      flag[i] = fl;
     }
     bsum<6>(s, red);
     const float cnt = s[3], mf = cnt > 0 ? s[4] / cnt : 0.f, mg = cnt > 0 ? s[5] / cnt : 0.f;
     float c[3] = {0, 0, 0};
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-      if (flags & (1u << (8 + q))) {
-        float a = fv[q] - mf, bb = gv[q] - mg;
+    for (int i = threadIdx.x; i < VT * VT; i += VNT)
+      if (flag[i] != 0.f) {
+        const int ly = i / VT, lx = i % VT;
+        float a = fdrr[i] - mf, bb = gres[(eh + ly) * E + eh + lx] - mg;
         c[0] = fmaf(a, a, c[0]);
         c[1] = fmaf(bb, bb, c[1]);
         c[2] = fmaf(a, bb, c[2]);
@@ -694,6 +868,7 @@ struct asc_engine_s {
   Bufs b{};
   size_t smem = 0;
   int sms = 152;
+  int view_blocks = 1;  // resident k_view blocks per SM
   bool prof = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   // device PSO: swarm state, the captured iteration and a private stream
@@ -819,7 +994,9 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
     hmax = std::max(hmax, std::max(S.views[v].h_drr, S.views[v].h_rad));
   }
   S.E = VT + 2 * hmax;
-  if (S.E > 120) {
+  // three E x E stage buffers and the final tile must fit one block's shared
+  // memory (227 KB less the static arrays)
+  if ((3 * S.E * S.E + VT * VT) * sizeof(float) > 224 * 1024) {
     delete e;
     return ASC_ERR_RANGE;
   }
@@ -894,10 +1071,12 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, dev);
   err = cudaFuncSetAttribute(k_view, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem);
+  if (!err) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->view_blocks, k_view, VNT, e->smem);
   if (err) {
     delete e;
     return cuda_status(err);
   }
+  e->view_blocks = std::max(e->view_blocks, 1);
   *out = e;
   return ASC_OK;
 }
@@ -937,9 +1116,9 @@ static int engine_launch(asc_engine e, int n, const int* bone, const double* man
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[0], s));
   k_setup<<<1, 1024, 0, s>>>(e->dev, n, bone, manip, e->b, cost, vcost);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[1], s));
-  k_ray<<<e->sms * 8, 256, 0, s>>>(e->dev, e->b, g_empty_skip);
+  k_ray<<<e->sms * ASC_RAY_MINBLOCKS, NRAY, 0, s>>>(e->dev, e->b, g_empty_skip);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[2], s));
-  k_view<<<e->sms * 4, 256, e->smem, s>>>(e->dev, e->b, cost, vcost);
+  k_view<<<e->sms * e->view_blocks, VNT, e->smem, s>>>(e->dev, e->b, cost, vcost);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[3], s));
   if (vcost) k_copy_vcost<<<8, 256, 0, s>>>(e->b.vcost, vcost, n * e->n_views);
   ASC_LAUNCH_CHECK();
@@ -967,6 +1146,18 @@ ASC_API int asc_engine_stats(asc_engine e, float ms[3], unsigned long long* samp
   ASC_CUDA(cudaMemcpy(&C, e->b.C, sizeof C, cudaMemcpyDeviceToHost));
   if (samples) *samples = C.samples;
   if (pixels) *pixels = C.pixels;
+  return ASC_OK;
+}
+
+ASC_API int asc_engine_counters(asc_engine e, unsigned long long out[4])
+{
+  if (!e || !out) return ASC_ERR_ARG;
+  Counters C;
+  ASC_CUDA(cudaMemcpy(&C, e->b.C, sizeof C, cudaMemcpyDeviceToHost));
+  out[0] = C.samples;
+  out[1] = C.pixels;
+  out[2] = C.marched;
+  out[3] = C.slots;
   return ASC_OK;
 }
 

@@ -251,23 +251,6 @@ __device__ __forceinline__ bool ray_setup(const float* m, const float* vp, int x
   return true;
 }
 
-// Integer base and FP32 fraction of coordinate C - k dC.  The march re-bases
-// at every multiple of REBASE samples, so that the fraction stays small
-// (|fraction| < 1 + REBASE |d|, exact to a few 1e-6 voxel) and a sample's
-// coordinates depend on its index k alone, whatever was skipped before it.
-#ifndef ASC_REBASE
-#define ASC_REBASE 64
-#endif
-constexpr int REBASE = ASC_REBASE;
-__device__ __forceinline__ void coord_base(df C, df dC, float k, int& base_i, float& base_f, float& frac)
-{
-  const df c = df_add(C, df_neg(df_mulf(dC, k)));
-  const float fl = floorf(c.h);
-  base_f = fl;
-  base_i = (int)fminf(fmaxf(fl, -1.0e6f), 1.0e6f);
-  frac = __fadd_rn(__fadd_rn(c.h, -fl), c.l);
-}
-
 // Index of the occupancy cell holding the lower tap of a sample at
 // (approximate) texel coordinates X, Y, Z: floor(X / OCC) per axis, clamped.
 __device__ __forceinline__ int occ_cell(float X, float Y, float Z, int bx, int by, int bz, int& cx, int& cy, int& cz)
@@ -278,118 +261,208 @@ __device__ __forceinline__ int occ_cell(float X, float Y, float Z, int bx, int b
   return (cz * by + cy) * bx + cx;
 }
 
-// Whole samples, after the current one, that stay in cell c along the march
-// (dir = +1: towards near, coordinates move by -d per sample; dir = -1: back
-// towards far).  A 1e-3 voxel margin covers the ~1e-4 error of the FP32
-// coordinates used here.
-__device__ __forceinline__ int cell_run(float X, float Y, float Z, float dX, float dY, float dZ, int cx, int cy, int cz,
-                                        float dir)
+// A ray's walk through the occupancy grid: FP32 coordinates at sample 0, their
+// decrease per sample and its reciprocal (0 where the decrease is 0).  These
+// approximate the double-float set-up to ~1e-4 voxel, well inside the 1e-3
+// voxel margin of cell_run.
+struct CellWalk {
+  float X, Y, Z, dX, dY, dZ, iX, iY, iZ;
+  int bx, by, bz;
+};
+
+__device__ __forceinline__ CellWalk cell_walk(const DevVolume& V, const RaySetup& r)
 {
+  CellWalk w;
+  w.X = r.X.h;
+  w.Y = r.Y.h;
+  w.Z = r.Z.h;
+  w.dX = r.dX.h;
+  w.dY = r.dY.h;
+  w.dZ = r.dZ.h;
+  w.iX = w.dX != 0.f ? 1.0f / w.dX : 0.f;
+  w.iY = w.dY != 0.f ? 1.0f / w.dY : 0.f;
+  w.iZ = w.dZ != 0.f ? 1.0f / w.dZ : 0.f;
+  w.bx = (V.nx + OCC - 1) / OCC;
+  w.by = (V.ny + OCC - 1) / OCC;
+  w.bz = (V.nz + OCC - 1) / OCC;
+  return w;
+}
+
+// Cell of sample k, and the whole samples after k (dir = +1: towards near,
+// coordinates move by -d per sample; dir = -1: back towards far) whose lower
+// tap stays at least 1e-3 voxel inside that cell.
+__device__ __forceinline__ int cell_step(const CellWalk& w, int k, float dir, int& cell)
+{
+  const float kf = (float)k;
+  const float X = fmaf(-kf, w.dX, w.X), Y = fmaf(-kf, w.dY, w.Y), Z = fmaf(-kf, w.dZ, w.Z);
+  int cx, cy, cz;
+  cell = occ_cell(X, Y, Z, w.bx, w.by, w.bz, cx, cy, cz);
   const float G = 1.0e-3f;
-  const float ex = dX * dir, ey = dY * dir, ez = dZ * dir;  // coordinate decrease per sample
   float s = 3.0e38f;
-  if (ex > 0.f) s = fminf(s, (X - (float)(OCC * cx) - G) / ex);
-  if (ex < 0.f) s = fminf(s, (X - (float)(OCC * cx + OCC) + G) / ex);
-  if (ey > 0.f) s = fminf(s, (Y - (float)(OCC * cy) - G) / ey);
-  if (ey < 0.f) s = fminf(s, (Y - (float)(OCC * cy + OCC) + G) / ey);
-  if (ez > 0.f) s = fminf(s, (Z - (float)(OCC * cz) - G) / ez);
-  if (ez < 0.f) s = fminf(s, (Z - (float)(OCC * cz + OCC) + G) / ez);
+  const float ex = w.dX * dir, ey = w.dY * dir, ez = w.dZ * dir;  // coordinate decrease per step
+  if (ex > 0.f) s = fminf(s, (X - (float)(OCC * cx) - G) * w.iX * dir);
+  if (ex < 0.f) s = fminf(s, (X - (float)(OCC * cx + OCC) + G) * w.iX * dir);
+  if (ey > 0.f) s = fminf(s, (Y - (float)(OCC * cy) - G) * w.iY * dir);
+  if (ey < 0.f) s = fminf(s, (Y - (float)(OCC * cy + OCC) + G) * w.iY * dir);
+  if (ez > 0.f) s = fminf(s, (Z - (float)(OCC * cz) - G) * w.iZ * dir);
+  if (ez < 0.f) s = fminf(s, (Z - (float)(OCC * cz + OCC) + G) * w.iZ * dir);
   return (int)fminf(fmaxf(floorf(s), 0.f), 1.0e7f);
 }
 
 // The first and last samples of a ray whose lower tap lies in an occupied
 // cell; the samples outside [k0, k1] add exactly nothing.  Returns false
-// when none is occupied.
+// when none is occupied.  Without `occ`, the whole ray.
 __device__ __forceinline__ bool occupied_span(const DevVolume& V, const uint8_t* __restrict__ occ, const RaySetup& r,
                                               int& k0, int& k1)
 {
   k0 = 0;
   k1 = r.K - 1;
   if (!occ || r.K <= 0) return r.K > 0;
-  const int bx = (V.nx + OCC - 1) / OCC, by = (V.ny + OCC - 1) / OCC, bz = (V.nz + OCC - 1) / OCC;
-  const float Xh = r.X.h, Yh = r.Y.h, Zh = r.Z.h, dX = r.dX.h, dY = r.dY.h, dZ = r.dZ.h;
-  int cx, cy, cz;
+  const CellWalk w = cell_walk(V, r);
+  int cell;
   for (;;) {  // from far towards near
-    const float kf = (float)k0;
-    const float X = fmaf(-kf, dX, Xh), Y = fmaf(-kf, dY, Yh), Z = fmaf(-kf, dZ, Zh);
-    if (__ldg(occ + occ_cell(X, Y, Z, bx, by, bz, cx, cy, cz))) break;
-    k0 += cell_run(X, Y, Z, dX, dY, dZ, cx, cy, cz, 1.0f) + 1;
+    const int run = cell_step(w, k0, 1.0f, cell);
+    if (__ldg(occ + cell)) break;
+    k0 += run + 1;
     if (k0 >= r.K) return false;
   }
   for (;;) {  // from near back towards far
-    const float kf = (float)k1;
-    const float X = fmaf(-kf, dX, Xh), Y = fmaf(-kf, dY, Yh), Z = fmaf(-kf, dZ, Zh);
-    if (__ldg(occ + occ_cell(X, Y, Z, bx, by, bz, cx, cy, cz))) break;
-    k1 -= cell_run(X, Y, Z, dX, dY, dZ, cx, cy, cz, -1.0f) + 1;
+    const int run = cell_step(w, k1, -1.0f, cell);
+    if (__ldg(occ + cell)) break;
+    k1 -= run + 1;
     if (k1 < k0) return false;  // cannot happen: k0 is occupied
   }
   return true;
 }
 
-// One ray of cuda_volume_render_kernel (RayCaster_kernels.cu:187-195): the
-// samples k0..k1 of the ray (t = far - k).  Returns the compensated (Kahan)
-// sum of raw samples above cutoff_raw (the caller scales by
-// step * norm / intensity).  Sample positions depend on k alone (bases at
-// multiples of REBASE), so the span [k0, k1] chosen by occupied_span changes
-// no bit of the result.
+// Within samples [lo, hi] (one march block), the first and last whose lower
+// tap lies in an occupied cell; false when there is none.  Without `occ`,
+// [lo, hi] itself.
+__device__ __forceinline__ bool block_extent(const CellWalk& w, const uint8_t* __restrict__ occ, int lo, int hi,
+                                             int& first, int& last)
+{
+  if (!occ) {
+    first = lo;
+    last = hi;
+    return lo <= hi;
+  }
+  first = -1;
+  last = -1;
+  for (int k = lo; k <= hi;) {
+    int cell;
+    const int run = cell_step(w, k, 1.0f, cell);
+    if (__ldg(occ + cell)) {
+      if (first < 0) first = k;
+      last = min(k + run, hi);
+    }
+    k += run + 1;
+  }
+  return first >= 0;
+}
+
+// Integer base and FP32 fraction of coordinate C - k dC.  The march re-bases
+// at every multiple of REBASE samples, so that the fraction stays small
+// (|fraction| < 1 + REBASE |d|, exact to a few 1e-6 voxel) and a sample's
+// coordinates depend on its index k alone.
+#ifndef ASC_REBASE
+#define ASC_REBASE 64
+#endif
+constexpr int REBASE = ASC_REBASE;
+__device__ __forceinline__ void coord_base(df C, df dC, float k, int& base_i, float& frac)
+{
+  const df c = df_add(C, df_neg(df_mulf(dC, k)));
+  const float fl = floorf(c.h);
+  base_i = (int)fminf(fmaxf(fl, -1.0e6f), 1.0e6f);
+  frac = __fadd_rn(__fadd_rn(c.h, -fl), c.l);
+}
+
+// Samples kb + js .. kb + je of one march block (kb a multiple of REBASE) of
+// cuda_volume_render_kernel's loop (RayCaster_kernels.cu:187-195; t = far -
+// k).  Returns the block's compensated (Kahan) sum of raw samples above
+// cutoff_raw as (sum, compensation); a sample at or below the cutoff leaves
+// both untouched, so trimming samples that add nothing changes no bit.
 template <int STORE>
-__device__ __forceinline__ float march(const DevVolume& V, const RaySetup& r, int k0, int k1, float cutoff_raw)
+__device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup& r, int kb, int js, int je,
+                                              float cutoff_raw)
 {
   const uint32_t* __restrict__ P = V.pairs;
   const int px = V.px, pxy = V.pxy;
   const unsigned xmax = (unsigned)(px - 1), ymax = (unsigned)(V.ny + 2 * PAD - 2),
                  zmax = (unsigned)(V.nz + 2 * PAD - 2);
   const float dXh = r.dX.h, dYh = r.dY.h, dZh = r.dZ.h;
+  int bix, biy, biz;
+  float fx, fy, fz;
+  const float kbf = (float)kb;
+  coord_base(r.X, r.dX, kbf, bix, fx);
+  coord_base(r.Y, r.dY, kbf, biy, fy);
+  coord_base(r.Z, r.dZ, kbf, biz, fz);
+  // padded indices of the lower taps are base + PAD + tap(fraction)
+  bix += PAD;
+  biy += PAD;
+  biz += PAD;
   float acc = 0.f, comp = 0.f;
-  for (int kb = k0 & ~(REBASE - 1); kb <= k1; kb += REBASE) {
-    int bix, biy, biz;
-    float bfx, bfy, bfz, fx, fy, fz;
-    const float kbf = (float)kb;
-    coord_base(r.X, r.dX, kbf, bix, bfx, fx);
-    coord_base(r.Y, r.dY, kbf, biy, bfy, fy);
-    coord_base(r.Z, r.dZ, kbf, biz, bfz, fz);
-    // padded indices of the lower taps are base + PAD + tap(fraction)
-    bix += PAD;
-    biy += PAD;
-    biz += PAD;
-    const int ke = min(kb + REBASE - 1, k1);
-    int k = max(kb, k0);
-    float j = (float)(k - kb);
-    for (; k <= ke; ++k, j += 1.0f) {
-      // j * (low part of d) stays below 1e-6 voxel for j < REBASE
-      int ix, iy, iz;
-      float ax, ay, az;
-      tap(fmaf(-j, dXh, fx), ix, ax);
-      tap(fmaf(-j, dYh, fy), iy, ay);
-      tap(fmaf(-j, dZh, fz), iz, az);
-      // inside the box the taps stay in the padded grid; the clamps only keep
-      // degenerate input in bounds
-      const unsigned xp = min((unsigned)(ix + bix), xmax);
-      const unsigned yp = min((unsigned)(iy + biy), ymax);
-      const unsigned zp = min((unsigned)(iz + biz), zmax);
-      const uint32_t* p0 = P + (size_t)zp * pxy + yp * px + xp;
-      const uint32_t w00 = __ldg(p0), w10 = __ldg(p0 + px), w01 = __ldg(p0 + pxy), w11 = __ldg(p0 + pxy + px);
-      float a0, a1, b0, b1, c0, c1, d0, d1;
-      unpack<STORE>(w00, a0, a1);
-      unpack<STORE>(w10, b0, b1);
-      unpack<STORE>(w01, c0, c1);
-      unpack<STORE>(w11, d0, d1);
-      const float e00 = fmaf(ax, a1 - a0, a0);
-      const float e10 = fmaf(ax, b1 - b0, b0);
-      const float e01 = fmaf(ax, c1 - c0, c0);
-      const float e11 = fmaf(ax, d1 - d0, d0);
-      const float f0 = fmaf(ay, e10 - e00, e00);
-      const float f1 = fmaf(ay, e11 - e01, e01);
-      const float s = fmaf(az, f1 - f0, f0);
-      if (s > cutoff_raw) {  // a sample at or below the cutoff leaves the sum untouched
-        const float y = s - comp;
-        const float tt = acc + y;
-        comp = (tt - acc) - y;
-        acc = tt;
-      }
+  float j = (float)js;
+  for (int k = js; k <= je; ++k, j += 1.0f) {
+    // j * (low part of d) stays below 1e-6 voxel for j < REBASE
+    int ix, iy, iz;
+    float ax, ay, az;
+    tap(fmaf(-j, dXh, fx), ix, ax);
+    tap(fmaf(-j, dYh, fy), iy, ay);
+    tap(fmaf(-j, dZh, fz), iz, az);
+    // inside the box the taps stay in the padded grid; the clamps only keep
+    // degenerate input in bounds
+    const unsigned xp = min((unsigned)(ix + bix), xmax);
+    const unsigned yp = min((unsigned)(iy + biy), ymax);
+    const unsigned zp = min((unsigned)(iz + biz), zmax);
+    const uint32_t* p0 = P + (size_t)zp * pxy + yp * px + xp;
+    const uint32_t w00 = __ldg(p0), w10 = __ldg(p0 + px), w01 = __ldg(p0 + pxy), w11 = __ldg(p0 + pxy + px);
+    float a0, a1, b0, b1, c0, c1, d0, d1;
+    unpack<STORE>(w00, a0, a1);
+    unpack<STORE>(w10, b0, b1);
+    unpack<STORE>(w01, c0, c1);
+    unpack<STORE>(w11, d0, d1);
+    const float e00 = fmaf(ax, a1 - a0, a0);
+    const float e10 = fmaf(ax, b1 - b0, b0);
+    const float e01 = fmaf(ax, c1 - c0, c0);
+    const float e11 = fmaf(ax, d1 - d0, d0);
+    const float f0 = fmaf(ay, e10 - e00, e00);
+    const float f1 = fmaf(ay, e11 - e01, e01);
+    const float s = fmaf(az, f1 - f0, f0);
+    if (s > cutoff_raw) {
+      const float y = s - comp;
+      const float tt = acc + y;
+      comp = (tt - acc) - y;
+      acc = tt;
     }
   }
-  return acc;
+  return make_float2(acc, comp);
+}
+
+// Adds a block's compensated sum (value sum - compensation) to the ray's
+// double-float total; blocks that added nothing leave it untouched.
+__device__ __forceinline__ void add_block(df& total, float2 p)
+{
+  if (p.x != 0.f || p.y != 0.f) total = df_add(df_add(total, df{p.x, 0.f}), df{-p.y, 0.f});
+}
+
+// One whole ray: the march blocks that hold occupied samples, in order, each
+// trimmed to its occupied extent, their sums combined in double-float.  The
+// result depends only on the samples above the cutoff, so it is the same
+// with and without `occ`, and the same as the batched engine's.
+template <int STORE>
+__device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __restrict__ occ, const RaySetup& r,
+                                       float cutoff_raw)
+{
+  int k0, k1;
+  if (!occupied_span(V, occ, r, k0, k1)) return 0.f;
+  const CellWalk w = cell_walk(V, r);
+  df total{0.f, 0.f};
+  for (int kb = k0 & ~(REBASE - 1); kb <= k1; kb += REBASE) {
+    int first, last;
+    if (block_extent(w, occ, max(kb, k0), min(kb + REBASE - 1, k1), first, last))
+      add_block(total, march_block<STORE>(V, r, kb, first - kb, last - kb, cutoff_raw));
+  }
+  return total.h + total.l;
 }
 
 }  // namespace asc

@@ -67,10 +67,8 @@ __global__ void __launch_bounds__(256) k_raycast(DevVolume V, const uint8_t* __r
   if (x >= w || y >= h) return;
   RaySetup r;
   float d = 0.f;
-  if (ray_setup(a.m, a.vp, x, y, df{a.sx[0], a.sx[1]}, df{a.sy[0], a.sy[1]}, a.step, V.nx, V.ny, V.nz, r)) {
-    int k0, k1;
-    if (occupied_span(V, occ, r, k0, k1)) d = march<STORE>(V, r, k0, k1, a.cutoff_raw) * a.scale;
-  }
+  if (ray_setup(a.m, a.vp, x, y, df{a.sx[0], a.sx[1]}, df{a.sy[0], a.sy[1]}, a.step, V.nx, V.ny, V.nz, r))
+    d = march<STORE>(V, occ, r, a.cutoff_raw) * a.scale;
   out[(size_t)y * w + x] = fminf(fmaxf(d, 0.f), 1.f);
 }
 

@@ -55,10 +55,14 @@ class Job:
         return self.finish - self.arrival
 
 
+PAD = 2  # edge voxels the device layout adds on every side
+
+
 def volume_bytes(vol: S.Volume) -> int:
+    """Device bytes of a volume: padded x-paired words plus occupancy grids."""
     D, H, W = vol.data.shape
     cells = ((W + 7) // 8) * ((H + 7) // 8) * ((D + 7) // 8)
-    return 4 * W * H * D + 4 * cells
+    return 4 * (W + 2 * PAD) * (H + 2 * PAD) * (D + 2 * PAD) + 4 * cells
 
 
 def engine_bytes(scene: S.Scene, max_items: int) -> int:
@@ -103,7 +107,7 @@ class VolumeCache:
         freed = 0
         with self.lock:
             for s in [s for s, r in self.refs.items() if r == 0]:
-                freed += sum(4 * int(np.prod(v.dims)) for v in self.entries[s])
+                freed += sum(4 * int(np.prod(np.asarray(v.dims) + 2 * PAD)) for v in self.entries[s])
                 del self.entries[s]
                 del self.refs[s]
         return freed

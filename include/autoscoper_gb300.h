@@ -252,6 +252,12 @@ int asc_engine_debug(asc_engine e, const float **drr_dev, const int **layout_dev
  * counts (the work figures of the roofline). */
 int asc_engine_profile(asc_engine e, int enable);
 int asc_engine_stats(asc_engine e, float ms[3], unsigned long long *samples, unsigned long long *pixels);
+/* Ray-cast work counters of the last evaluation: out[0] trilinear samples of
+ * the reference's march (far to near over the whole box), out[1] pixels,
+ * out[2] samples actually marched after empty-space skipping, out[3] lane
+ * slots the marching warps occupied (32 x the longest marched span of each
+ * warp's rays); out[2] / out[3] is the SIMT efficiency of the march. */
+int asc_engine_counters(asc_engine e, unsigned long long out[4]);
 
 /* ---- device-resident optimizers ----
  * Synchronous batched PSO over all bones at once: n_particles per bone,

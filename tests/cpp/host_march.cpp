@@ -59,10 +59,8 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
       df_split((double)vp[3] / (double)h, sy.h, sy.l);
       if (ray_setup(m, vp, x, y, sx, sy, step, nx, ny, nz, r)) {
         const uint8_t* o = skip ? occ.data() : nullptr;
-        int k0, k1;
-        float acc = 0.f;
-        if (occupied_span(V, o, r, k0, k1))
-          acc = storage == ASC_STORE_BF16 ? march<ASC_STORE_BF16>(V, r, k0, k1, cut) : march<ASC_STORE_U16>(V, r, k0, k1, cut);
+        const float acc =
+            storage == ASC_STORE_BF16 ? march<ASC_STORE_BF16>(V, o, r, cut) : march<ASC_STORE_U16>(V, o, r, cut);
         d = acc * (step * V.norm / intensity);
         n = r.K;
       }

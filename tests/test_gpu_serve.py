@@ -40,5 +40,5 @@ def test_admission_respects_budget():
     budget = 1.5 * need + 2e9  # room for about one job at a time
     srv = serve.Server(hbm_budget=budget, slots=4)
     summary = srv.serve(jobs, realtime=False)
-    assert summary["failed"] == 0
+    assert summary["failed"] == 0, [j.error for j in jobs]
     assert srv.peak <= budget
