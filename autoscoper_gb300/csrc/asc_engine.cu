@@ -46,8 +46,7 @@ constexpr int VT = ASC_VT;   // k_view output tile edge
 constexpr int VNT = 256;     // k_view threads per block
 constexpr int RTX = 16, RTY = 16;  // k_ray work item: one block, 16 x 16 rays
 constexpr int NRAY = RTX * RTY;    // k_ray threads per block, one ray each
-constexpr int NBW = 8;             // march blocks per ray per k_ray pass
-constexpr int SEGCAP = 1024;       // march segments per k_ray pass
+constexpr int NBW = 8;             // march segments per ray per k_ray pass
 
 struct FilterDev {
   int kind, K, R;
@@ -262,16 +261,15 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
 
 // Rays of one 16 x 16 tile of one (item, view) crop per block.  Each ray's
 // march is cut into segments: the REBASE-sample march blocks that hold
-// occupied samples, each trimmed to its occupied extent (block_extent).  The
-// block's segments are sorted by length (counting sort, longest first) and
-// marched 32 at a time by whichever warp is free, so the lanes of a warp
-// march segments of nearly equal length whatever the rays' lengths; each
-// ray then adds its blocks' sums in order (add_block), as march() does for
-// a single ray.  A ray with more than NBW blocks, or a tile with more than
-// SEGCAP segments, takes further passes.
+// occupied samples, each trimmed to its occupied extent (walk_segments).
+// The block's segments are sorted by length (counting sort, longest first)
+// and marched 32 at a time by whichever warp is free, so the lanes of a warp
+// march segments of nearly equal length whatever the rays' lengths; each ray
+// then adds its blocks' sums in order (add_block), as march() does for a
+// single ray.  A ray with more than NBW segments takes further passes.
 template <int STORE>
-__device__ __forceinline__ void march_segments(const DevVolume& V, const float4 (*rec)[NRAY], const int* b0,
-                                               const unsigned* ord, float2* part, int nseg, int* grab, float cut,
+__device__ __forceinline__ void march_segments(const DevVolume& V, const float4 (*rec)[NRAY], const unsigned* ord,
+                                               float2* part, int nseg, int* grab, float cut,
                                                unsigned long long& marched, unsigned long long& slots)
 {
   const unsigned FULL = 0xffffffffu;
@@ -294,7 +292,7 @@ __device__ __forceinline__ void march_segments(const DevVolume& V, const float4 
       r.dX = df{q1.z, q1.w};
       r.dY = df{q2.x, q2.y};
       r.dZ = df{q2.z, q2.w};
-      const int kb = (b0[ray] + slot % NBW) * REBASE;
+      const int kb = __float_as_int(part[slot].x);  // the block start, until the sum replaces it
       part[slot] = march_block<STORE>(V, r, kb, js, je, cut);
       len = je - js + 1;
     }
@@ -308,10 +306,9 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
 {
   static_assert(REBASE == 64 && NRAY * NBW <= 2048, "segment fields: 11-bit slot, 6-bit offsets");
   __shared__ float4 s_rec[3][NRAY];      // per ray: X, Y, Z, dX, dY, dZ as double-floats
-  __shared__ float2 s_part[NRAY * NBW];  // per ray and march block: (sum, compensation)
-  __shared__ unsigned s_seg[SEGCAP];     // segments: slot | js << 11 | je << 17
-  __shared__ unsigned s_ord[SEGCAP];     // the same, longest first
-  __shared__ int s_b0[NRAY];             // first march block of each ray in this pass
+  __shared__ float2 s_part[NRAY * NBW];  // per segment slot: block start, then (sum, compensation)
+  __shared__ unsigned s_seg[NRAY * NBW]; // per segment slot: slot | js << 11 | je << 17
+  __shared__ unsigned s_ord[NRAY * NBW]; // the segments, longest first
   __shared__ int s_cnt[REBASE];          // segments per length - 1, then placement cursors
   __shared__ int s_tile, s_nseg, s_grab;
   const unsigned FULL = 0xffffffffu;
@@ -340,43 +337,32 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
       const unsigned tot = __reduce_add_sync(FULL, hit ? (unsigned)rs.K : 0u);
       if (lane == 0) atomicAdd(&b.C->samples, (unsigned long long)tot);
     }
-    int kw = 1, kend = 0;  // samples still to walk: [kw, kend]
-    if (hit && occupied_span(B.vol, occ, rs, kw, kend)) {
+    bool done = true;
+    if (hit && rs.K > 0) {
       s_rec[0][tid] = make_float4(rs.X.h, rs.X.l, rs.Y.h, rs.Y.l);
       s_rec[1][tid] = make_float4(rs.Z.h, rs.Z.l, rs.dX.h, rs.dX.l);
       s_rec[2][tid] = make_float4(rs.dY.h, rs.dY.l, rs.dZ.h, rs.dZ.l);
-    } else {
-      kw = 1;
-      kend = 0;
+      done = false;
     }
-    const CellWalk cw = cell_walk(B.vol, rs);
+    CellWalk cw = cell_walk(B.vol, rs, 0);
+    WalkState ws{0, rs.K - 1, 0, -1, 0};
     df total{0.f, 0.f};
     for (;;) {
       if (tid < REBASE) s_cnt[tid] = 0;
-      if (tid == 0) {
-        s_nseg = 0;
-        s_grab = 0;
-      }
+      if (tid == 0) s_grab = 0;
       __syncthreads();
-      // ---- walk: this pass's segments of this ray
-      unsigned mask = 0;
-      const int b0 = kw / REBASE;
-      s_b0[tid] = b0;
-      while (kw <= kend) {
-        const int kb = (kw / REBASE) * REBASE, i = kw / REBASE - b0;
-        if (i >= NBW) break;
-        int first, last;
-        if (block_extent(cw, occ, kw, min(kb + REBASE - 1, kend), first, last)) {
-          const int at = atomicAdd(&s_nseg, 1);
-          if (at >= SEGCAP) break;  // resume at this block in the next pass
-          s_seg[at] = (unsigned)(tid * NBW + i) | (unsigned)(first - kb) << 11 | (unsigned)(last - kb) << 17;
-          atomicAdd(&s_cnt[last - first], 1);
-          mask |= 1u << i;
-        }
-        kw = kb + REBASE;
-      }
+      // ---- walk: up to NBW segments of this ray
+      int n = 0;
+      if (!done)
+        done = walk_segments(cw, occ, ws, [&](int kb, int js, int je) {
+          if (n == NBW) return false;
+          const int slot = tid * NBW + n++;
+          s_seg[slot] = (unsigned)slot | (unsigned)js << 11 | (unsigned)je << 17;
+          s_part[slot].x = __int_as_float(kb);
+          atomicAdd(&s_cnt[je - js], 1);
+          return true;
+        });
       __syncthreads();
-      const int nseg = min(s_nseg, SEGCAP);
       // ---- counting sort by length, longest first
       if (tid < 32) {
         const int c0 = s_cnt[REBASE - 1 - 2 * lane], c1 = s_cnt[REBASE - 2 - 2 * lane];
@@ -388,26 +374,27 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
         const int excl = incl - c0 - c1;
         s_cnt[REBASE - 1 - 2 * lane] = excl;
         s_cnt[REBASE - 2 - 2 * lane] = excl + c0;
+        if (lane == 31) s_nseg = incl;
       }
       __syncthreads();
-      for (int i = tid; i < nseg; i += NRAY) {
-        const unsigned d = s_seg[i];
+      for (int i = 0; i < n; ++i) {
+        const unsigned d = s_seg[tid * NBW + i];
         const int len1 = (int)((d >> 17) & 63u) - (int)((d >> 11) & 63u);
         s_ord[atomicAdd(&s_cnt[len1], 1)] = d;
       }
       __syncthreads();
+      const int nseg = s_nseg;
       // ---- march the segments, 32 at a time per warp
       if (B.vol.storage == ASC_STORE_BF16)
-        march_segments<ASC_STORE_BF16>(B.vol, s_rec, s_b0, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
+        march_segments<ASC_STORE_BF16>(B.vol, s_rec, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
       else if (B.vol.storage == ASC_STORE_F16)
-        march_segments<ASC_STORE_F16>(B.vol, s_rec, s_b0, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
+        march_segments<ASC_STORE_F16>(B.vol, s_rec, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
       else
-        march_segments<ASC_STORE_U16>(B.vol, s_rec, s_b0, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
+        march_segments<ASC_STORE_U16>(B.vol, s_rec, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
       __syncthreads();
-      // ---- this ray's blocks, in order
-      for (int i = 0; i < NBW; ++i)
-        if (mask >> i & 1u) add_block(total, s_part[tid * NBW + i]);
-      if (!__syncthreads_or(kw <= kend)) break;
+      // ---- this ray's segments, in order
+      for (int i = 0; i < n; ++i) add_block(total, s_part[tid * NBW + i]);
+      if (!__syncthreads_or(!done)) break;
     }
     if (valid) b.drr[r.pix + (long long)y * r.w + x] = fminf(fmaxf((total.h + total.l) * B.scale[v], 0.f), 1.f);
   }

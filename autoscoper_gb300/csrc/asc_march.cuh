@@ -70,23 +70,44 @@ __device__ __forceinline__ void unpack(uint32_t w, float& lo, float& hi)
 }
 
 // Index and weight of the lower tap of a linear filter at voxel coordinate
-// X (texel centres at integers): k = nearest integer to X - 0.5, a = X - k in
-// [0, 1].  Where X is an integer the tie may give k = floor(X) - 1 with
-// a = 1, which selects the same value.
+// X (texel centres at integers, |X| < 2^22): k = floor(X), a = X - k in
+// [0, 1).  M + X rounded down is M + floor(X), an integer whose bits are
+// those of M plus floor(X).
 __device__ __forceinline__ void tap(float X, int& k, float& a)
 {
   const float M = 12582912.0f;  // 1.5 * 2^23
-  float t = __fadd_rn(__fadd_rn(X, -0.5f), M);
+  const float t = __fadd_rd(X, M);
   k = __float_as_int(t) - 0x4b400000;
   a = __fadd_rn(X, -__fadd_rn(t, -M));
 }
 
+// Linear interpolation between the two halves of a paired word with weight
+// a on the high half.  For u16 halves the values stay biased by 2^23: the
+// biased values, their difference and the removal of the bias are exact in
+// FP32, so this equals fmaf(a, hi - lo, lo) of the unbiased values.
+template <int STORE>
+__device__ __forceinline__ float lerp_pair(uint32_t w, float a)
+{
+  if (STORE == ASC_STORE_U16) {
+    const float lo = __uint_as_float(0x4b000000u | (w & 0xffffu)), hi = __uint_as_float(0x4b000000u | (w >> 16));
+    return fmaf(a, hi - lo, lo - 8388608.0f);
+  } else {
+    float lo, hi;
+    unpack<STORE>(w, lo, hi);
+    return fmaf(a, hi - lo, lo);
+  }
+}
+
 // Occupancy of 8x8x8-voxel cells for one cutoff: cell (cx, cy, cz) is 0 when
-// every voxel of [8c-1, 8c+9) on each axis (the taps of any sample whose
-// lower tap lies in the cell) is <= cutoff.  A trilinear sample is a convex
-// combination of its taps, so such a sample is <= cutoff and adds exactly
-// nothing to the DRR (RayCaster_kernels.cu:189); the march skips it.
+// every voxel of [8c-1, 8c+10) on each axis is <= cutoff.  That range holds
+// the taps of nonzero weight of every sample at a texel coordinate in
+// (8c-1, 8c+9), i.e. within one voxel of the cell's own [8c, 8c+8), so a walk
+// may place a sample in a cell with an error of up to a voxel.  A trilinear
+// sample is a convex combination of its taps (each FP32 lerp stays between
+// its ends), so a sample placed in an empty cell is <= cutoff and adds
+// exactly nothing to the DRR (RayCaster_kernels.cu:189); the march skips it.
 constexpr int OCC = 8;
+constexpr int OCC_LO = 1, OCC_HI = 2;  // apron voxels below and above a cell
 
 
 // ---- double-float arithmetic: a value is the unevaluated sum h + l of two
@@ -251,123 +272,133 @@ __device__ __forceinline__ bool ray_setup(const float* m, const float* vp, int x
   return true;
 }
 
-// Index of the occupancy cell holding the lower tap of a sample at
-// (approximate) texel coordinates X, Y, Z: floor(X / OCC) per axis, clamped.
-__device__ __forceinline__ int occ_cell(float X, float Y, float Z, int bx, int by, int bz, int& cx, int& cy, int& cz)
-{
-  cx = min(max(__float2int_rd(X * (1.0f / OCC)), 0), bx - 1);
-  cy = min(max(__float2int_rd(Y * (1.0f / OCC)), 0), by - 1);
-  cz = min(max(__float2int_rd(Z * (1.0f / OCC)), 0), bz - 1);
-  return (cz * by + cy) * bx + cx;
-}
+// The march re-bases its FP32 coordinates every REBASE samples (march_block).
+#ifndef ASC_REBASE
+#define ASC_REBASE 64
+#endif
+constexpr int REBASE = ASC_REBASE;
 
-// A ray's walk through the occupancy grid: FP32 coordinates at sample 0, their
-// decrease per sample and its reciprocal (0 where the decrease is 0).  These
-// approximate the double-float set-up to ~1e-4 voxel, well inside the 1e-3
-// voxel margin of cell_run.
+// A ray's walk through the occupancy grid (a 3-D DDA over cells, in units of
+// samples): the sample index of each axis' next cell-plane crossing, the
+// samples between crossings and the cell step per crossing.  FP32 throughout:
+// a sample's cell comes out within ~1e-3 voxel of the exact one, far inside
+// the one-voxel apron of the occupancy grid.
 struct CellWalk {
-  float X, Y, Z, dX, dY, dZ, iX, iY, iZ;
-  int bx, by, bz;
+  float tx, ty, tz;     // next crossing per axis (sample index; +inf if none)
+  float dtx, dty, dtz;  // samples between crossings
+  int cx, cy, cz;       // current cell (unclamped)
+  int sx, sy, sz;       // cell index change per crossing
+  int bx, by, bz;       // grid size in cells
 };
 
-__device__ __forceinline__ CellWalk cell_walk(const DevVolume& V, const RaySetup& r)
+__device__ __forceinline__ void walk_axis(float C, float dC, float kf, float& t, float& dt, int& c, int& st)
+{
+  // coordinate at sample k: C - k dC
+  const float X = fmaf(-kf, dC, C);
+  c = __float2int_rd(X * (1.0f / OCC));
+  if (dC > 0.f) {  // decreasing: next plane at OCC * c
+    st = -1;
+    dt = OCC / dC;
+    t = kf + (X - (float)(OCC * c)) / dC;
+  } else if (dC < 0.f) {  // increasing: next plane at OCC * (c + 1)
+    st = 1;
+    dt = -OCC / dC;
+    t = kf + (X - (float)(OCC * (c + 1))) / dC;
+  } else {
+    st = 0;
+    dt = 3.0e38f;
+    t = 3.0e38f;
+  }
+}
+
+__device__ __forceinline__ CellWalk cell_walk(const DevVolume& V, const RaySetup& r, int k)
 {
   CellWalk w;
-  w.X = r.X.h;
-  w.Y = r.Y.h;
-  w.Z = r.Z.h;
-  w.dX = r.dX.h;
-  w.dY = r.dY.h;
-  w.dZ = r.dZ.h;
-  w.iX = w.dX != 0.f ? 1.0f / w.dX : 0.f;
-  w.iY = w.dY != 0.f ? 1.0f / w.dY : 0.f;
-  w.iZ = w.dZ != 0.f ? 1.0f / w.dZ : 0.f;
+  const float kf = (float)k;
+  walk_axis(r.X.h, r.dX.h, kf, w.tx, w.dtx, w.cx, w.sx);
+  walk_axis(r.Y.h, r.dY.h, kf, w.ty, w.dty, w.cy, w.sy);
+  walk_axis(r.Z.h, r.dZ.h, kf, w.tz, w.dtz, w.cz, w.sz);
   w.bx = (V.nx + OCC - 1) / OCC;
   w.by = (V.ny + OCC - 1) / OCC;
   w.bz = (V.nz + OCC - 1) / OCC;
   return w;
 }
 
-// Cell of sample k, and the whole samples after k (dir = +1: towards near,
-// coordinates move by -d per sample; dir = -1: back towards far) whose lower
-// tap stays at least 1e-3 voxel inside that cell.
-__device__ __forceinline__ int cell_step(const CellWalk& w, int k, float dir, int& cell)
-{
-  const float kf = (float)k;
-  const float X = fmaf(-kf, w.dX, w.X), Y = fmaf(-kf, w.dY, w.Y), Z = fmaf(-kf, w.dZ, w.Z);
-  int cx, cy, cz;
-  cell = occ_cell(X, Y, Z, w.bx, w.by, w.bz, cx, cy, cz);
-  const float G = 1.0e-3f;
-  float s = 3.0e38f;
-  const float ex = w.dX * dir, ey = w.dY * dir, ez = w.dZ * dir;  // coordinate decrease per step
-  if (ex > 0.f) s = fminf(s, (X - (float)(OCC * cx) - G) * w.iX * dir);
-  if (ex < 0.f) s = fminf(s, (X - (float)(OCC * cx + OCC) + G) * w.iX * dir);
-  if (ey > 0.f) s = fminf(s, (Y - (float)(OCC * cy) - G) * w.iY * dir);
-  if (ey < 0.f) s = fminf(s, (Y - (float)(OCC * cy + OCC) + G) * w.iY * dir);
-  if (ez > 0.f) s = fminf(s, (Z - (float)(OCC * cz) - G) * w.iZ * dir);
-  if (ez < 0.f) s = fminf(s, (Z - (float)(OCC * cz + OCC) + G) * w.iZ * dir);
-  return (int)fminf(fmaxf(floorf(s), 0.f), 1.0e7f);
-}
+// Walk state of one ray between calls of walk_segments: the next sample to
+// place, and the open march block (index pb, occupied extent [pf, pl]; pf < 0
+// when none is open).
+struct WalkState {
+  int k, kend;
+  int pb, pf, pl;
+};
 
-// The first and last samples of a ray whose lower tap lies in an occupied
-// cell; the samples outside [k0, k1] add exactly nothing.  Returns false
-// when none is occupied.  Without `occ`, the whole ray.
-__device__ __forceinline__ bool occupied_span(const DevVolume& V, const uint8_t* __restrict__ occ, const RaySetup& r,
-                                              int& k0, int& k1)
+// Walks samples s.k .. s.kend and hands each march block that holds occupied
+// samples to emit(kb, js, je) -- block start kb (a multiple of REBASE) and the
+// occupied extent [kb + js, kb + je] -- in increasing k.  emit returns false
+// when it can take no more; the walk then stops, and a later call resumes
+// where it stopped.  Returns true when the ray is done.  Without `occ` every
+// sample counts as occupied.  The steps are bounded by the cells the ray
+// crosses; past that bound the rest of the ray counts as occupied.
+template <class Emit>
+__device__ __forceinline__ bool walk_segments(CellWalk& w, const uint8_t* __restrict__ occ, WalkState& s, Emit&& emit)
 {
-  k0 = 0;
-  k1 = r.K - 1;
-  if (!occ || r.K <= 0) return r.K > 0;
-  const CellWalk w = cell_walk(V, r);
-  int cell;
-  for (;;) {  // from far towards near
-    const int run = cell_step(w, k0, 1.0f, cell);
-    if (__ldg(occ + cell)) break;
-    k0 += run + 1;
-    if (k0 >= r.K) return false;
+  int steps = 2 * (w.bx + w.by + w.bz) + 8;
+  while (s.k <= s.kend) {
+    int ke = s.kend;
+    bool full = true;
+    float tn = 3.0e38f;
+    if (occ && steps > 0) {
+      tn = fminf(w.tx, fminf(w.ty, w.tz));
+      if (tn < (float)s.kend) ke = (int)floorf(tn);
+      const int cx = min(max(w.cx, 0), w.bx - 1), cy = min(max(w.cy, 0), w.by - 1),
+                cz = min(max(w.cz, 0), w.bz - 1);
+      full = __ldg(occ + (cz * w.by + cy) * w.bx + cx) != 0;
+      --steps;
+    }
+    if (ke >= s.k) {
+      if (full) {
+        // add samples [a, ke] to the open block(s)
+        for (int a = s.k; a <= ke;) {
+          const int bb = a / REBASE, hi = min(ke, bb * REBASE + REBASE - 1);
+          if (s.pf >= 0 && s.pb != bb) {
+            if (!emit(s.pb * REBASE, s.pf - s.pb * REBASE, s.pl - s.pb * REBASE)) {
+              s.k = a;  // resume here; the walk state still describes this cell
+              return false;
+            }
+            s.pf = -1;
+          }
+          if (s.pf < 0) {
+            s.pb = bb;
+            s.pf = a;
+          }
+          s.pl = hi;
+          a = hi + 1;
+        }
+      }
+      s.k = ke + 1;
+    }
+    if (tn == w.tx) {
+      w.cx += w.sx;
+      w.tx += w.dtx;
+    } else if (tn == w.ty) {
+      w.cy += w.sy;
+      w.ty += w.dty;
+    } else {
+      w.cz += w.sz;
+      w.tz += w.dtz;
+    }
   }
-  for (;;) {  // from near back towards far
-    const int run = cell_step(w, k1, -1.0f, cell);
-    if (__ldg(occ + cell)) break;
-    k1 -= run + 1;
-    if (k1 < k0) return false;  // cannot happen: k0 is occupied
+  if (s.pf >= 0) {
+    if (!emit(s.pb * REBASE, s.pf - s.pb * REBASE, s.pl - s.pb * REBASE)) return false;
+    s.pf = -1;
   }
   return true;
-}
-
-// Within samples [lo, hi] (one march block), the first and last whose lower
-// tap lies in an occupied cell; false when there is none.  Without `occ`,
-// [lo, hi] itself.
-__device__ __forceinline__ bool block_extent(const CellWalk& w, const uint8_t* __restrict__ occ, int lo, int hi,
-                                             int& first, int& last)
-{
-  if (!occ) {
-    first = lo;
-    last = hi;
-    return lo <= hi;
-  }
-  first = -1;
-  last = -1;
-  for (int k = lo; k <= hi;) {
-    int cell;
-    const int run = cell_step(w, k, 1.0f, cell);
-    if (__ldg(occ + cell)) {
-      if (first < 0) first = k;
-      last = min(k + run, hi);
-    }
-    k += run + 1;
-  }
-  return first >= 0;
 }
 
 // Integer base and FP32 fraction of coordinate C - k dC.  The march re-bases
 // at every multiple of REBASE samples, so that the fraction stays small
 // (|fraction| < 1 + REBASE |d|, exact to a few 1e-6 voxel) and a sample's
 // coordinates depend on its index k alone.
-#ifndef ASC_REBASE
-#define ASC_REBASE 64
-#endif
-constexpr int REBASE = ASC_REBASE;
 __device__ __forceinline__ void coord_base(df C, df dC, float k, int& base_i, float& frac)
 {
   const df c = df_add(C, df_neg(df_mulf(dC, k)));
@@ -402,6 +433,7 @@ __device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup
   biz += PAD;
   float acc = 0.f, comp = 0.f;
   float j = (float)js;
+#pragma unroll 2
   for (int k = js; k <= je; ++k, j += 1.0f) {
     // j * (low part of d) stays below 1e-6 voxel for j < REBASE
     int ix, iy, iz;
@@ -416,15 +448,10 @@ __device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup
     const unsigned zp = min((unsigned)(iz + biz), zmax);
     const uint32_t* p0 = P + (size_t)zp * pxy + yp * px + xp;
     const uint32_t w00 = __ldg(p0), w10 = __ldg(p0 + px), w01 = __ldg(p0 + pxy), w11 = __ldg(p0 + pxy + px);
-    float a0, a1, b0, b1, c0, c1, d0, d1;
-    unpack<STORE>(w00, a0, a1);
-    unpack<STORE>(w10, b0, b1);
-    unpack<STORE>(w01, c0, c1);
-    unpack<STORE>(w11, d0, d1);
-    const float e00 = fmaf(ax, a1 - a0, a0);
-    const float e10 = fmaf(ax, b1 - b0, b0);
-    const float e01 = fmaf(ax, c1 - c0, c0);
-    const float e11 = fmaf(ax, d1 - d0, d0);
+    const float e00 = lerp_pair<STORE>(w00, ax);
+    const float e10 = lerp_pair<STORE>(w10, ax);
+    const float e01 = lerp_pair<STORE>(w01, ax);
+    const float e11 = lerp_pair<STORE>(w11, ax);
     const float f0 = fmaf(ay, e10 - e00, e00);
     const float f1 = fmaf(ay, e11 - e01, e01);
     const float s = fmaf(az, f1 - f0, f0);
@@ -453,15 +480,14 @@ template <int STORE>
 __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __restrict__ occ, const RaySetup& r,
                                        float cutoff_raw)
 {
-  int k0, k1;
-  if (!occupied_span(V, occ, r, k0, k1)) return 0.f;
-  const CellWalk w = cell_walk(V, r);
+  if (r.K <= 0) return 0.f;
+  CellWalk w = cell_walk(V, r, 0);
+  WalkState s{0, r.K - 1, 0, -1, 0};
   df total{0.f, 0.f};
-  for (int kb = k0 & ~(REBASE - 1); kb <= k1; kb += REBASE) {
-    int first, last;
-    if (block_extent(w, occ, max(kb, k0), min(kb + REBASE - 1, k1), first, last))
-      add_block(total, march_block<STORE>(V, r, kb, first - kb, last - kb, cutoff_raw));
-  }
+  walk_segments(w, occ, s, [&](int kb, int js, int je) {
+    add_block(total, march_block<STORE>(V, r, kb, js, je, cutoff_raw));
+    return true;
+  });
   return total.h + total.l;
 }
 

@@ -390,8 +390,8 @@ __global__ void __launch_bounds__(RB) k_hdist_sad(const float* __restrict__ f, c
   }
 }
 
-// Occupancy of 8^3-voxel cells (see OCC in asc_internal.cuh): one thread per
-// cell takes the maximum over its trilinear support.
+// Occupancy of 8^3-voxel cells (OCC, OCC_LO, OCC_HI in asc_march.cuh): one
+// thread per cell takes the maximum over the cell and its apron.
 template <int STORE>
 __global__ void k_occupancy(DevVolume V, float cutoff_raw, uint8_t* __restrict__ occ)
 {
@@ -400,9 +400,10 @@ __global__ void k_occupancy(DevVolume V, float cutoff_raw, uint8_t* __restrict__
   if (c >= bx * by * bz) return;
   const int cx = c % bx, cy = (c / bx) % by, cz = c / (bx * by);
   float mx = -1.0f;
-  for (int z = max(cz * OCC - 1, 0); z < min(cz * OCC + OCC + 1, V.nz); ++z)
-    for (int y = max(cy * OCC - 1, 0); y < min(cy * OCC + OCC + 1, V.ny); ++y)
-      for (int x = max(cx * OCC - 1, 0); x < min(cx * OCC + OCC + 1, V.nx); ++x) {
+  const int lo = -OCC_LO, hi = OCC + OCC_HI;
+  for (int z = max(cz * OCC + lo, 0); z < min(cz * OCC + hi, V.nz); ++z)
+    for (int y = max(cy * OCC + lo, 0); y < min(cy * OCC + hi, V.ny); ++y)
+      for (int x = max(cx * OCC + lo, 0); x < min(cx * OCC + hi, V.nx); ++x) {
         float lo, hi;
         unpack<STORE>(V.pairs[(size_t)(z + PAD) * V.pxy + (size_t)(y + PAD) * V.px + (x + PAD)], lo, hi);
         mx = fmaxf(mx, lo);

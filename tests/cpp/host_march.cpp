@@ -38,9 +38,9 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
     for (int cy = 0; cy < by; ++cy)
       for (int cx = 0; cx < bx; ++cx) {
         float mx = -1.0f;
-        for (int z = std::max(cz * OCC - 1, 0); z < std::min(cz * OCC + OCC + 1, nz); ++z)
-          for (int y = std::max(cy * OCC - 1, 0); y < std::min(cy * OCC + OCC + 1, ny); ++y)
-            for (int x = std::max(cx * OCC - 1, 0); x < std::min(cx * OCC + OCC + 1, nx); ++x) {
+        for (int z = std::max(cz * OCC - OCC_LO, 0); z < std::min(cz * OCC + OCC + OCC_HI, nz); ++z)
+          for (int y = std::max(cy * OCC - OCC_LO, 0); y < std::min(cy * OCC + OCC + OCC_HI, ny); ++y)
+            for (int x = std::max(cx * OCC - OCC_LO, 0); x < std::min(cx * OCC + OCC + OCC_HI, nx); ++x) {
               float lo, hi;
               uint32_t wd = pairs[(size_t)(z + PAD) * pxy + (size_t)(y + PAD) * px + (x + PAD)];
               if (storage == ASC_STORE_BF16) unpack<ASC_STORE_BF16>(wd, lo, hi);

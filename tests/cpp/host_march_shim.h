@@ -13,6 +13,14 @@ using std::max;
 using std::min;
 inline float __fadd_rn(float a, float b) { volatile float r = a + b; return r; }
 inline float __fmul_rn(float a, float b) { volatile float r = a * b; return r; }
+// a + b rounded towards -inf (the sum of two floats is exact in double here)
+inline float __fadd_rd(float a, float b)
+{
+  const double s = (double)a + (double)b;
+  float f = (float)s;
+  if ((double)f > s) f = std::nextafter(f, -INFINITY);
+  return f;
+}
 inline float __fdiv_rn(float a, float b) { volatile float r = a / b; return r; }
 inline float __fsqrt_rn(float a) { return std::sqrt(a); }
 inline float __frcp_rn(float a) { volatile float r = 1.0f / a; return r; }
