@@ -69,18 +69,6 @@ __device__ __forceinline__ void unpack(uint32_t w, float& lo, float& hi)
   }
 }
 
-// Index and weight of the lower tap of a linear filter at voxel coordinate
-// X (texel centres at integers, |X| < 2^22): k = floor(X), a = X - k in
-// [0, 1).  M + X rounded down is M + floor(X), an integer whose bits are
-// those of M plus floor(X).
-__device__ __forceinline__ void tap(float X, int& k, float& a)
-{
-  const float M = 12582912.0f;  // 1.5 * 2^23
-  const float t = __fadd_rd(X, M);
-  k = __float_as_int(t) - 0x4b400000;
-  a = __fadd_rn(X, -__fadd_rn(t, -M));
-}
-
 // Linear interpolation between the two halves of a paired word with weight
 // a on the high half.  For u16 halves the values stay biased by 2^23: the
 // biased values, their difference and the removal of the bias are exact in
@@ -89,7 +77,9 @@ template <int STORE>
 __device__ __forceinline__ float lerp_pair(uint32_t w, float a)
 {
   if (STORE == ASC_STORE_U16) {
-    const float lo = __uint_as_float(0x4b000000u | (w & 0xffffu)), hi = __uint_as_float(0x4b000000u | (w >> 16));
+    // 2^23 + v: the half's two bytes under the exponent byte 0x4b
+    const float lo = __uint_as_float(__byte_perm(w, 0x4b000000u, 0x7610)),
+                hi = __uint_as_float(__byte_perm(w, 0x4b000000u, 0x7632));
     return fmaf(a, hi - lo, lo - 8388608.0f);
   } else {
     float lo, hi;
@@ -417,9 +407,7 @@ __device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup
                                               float cutoff_raw)
 {
   const uint32_t* __restrict__ P = V.pairs;
-  const int px = V.px, pxy = V.pxy;
-  const unsigned xmax = (unsigned)(px - 1), ymax = (unsigned)(V.ny + 2 * PAD - 2),
-                 zmax = (unsigned)(V.nz + 2 * PAD - 2);
+  const unsigned px = (unsigned)V.px, pxy = (unsigned)V.pxy;
   const float dXh = r.dX.h, dYh = r.dY.h, dZh = r.dZ.h;
   int bix, biy, biz;
   float fx, fy, fz;
@@ -427,26 +415,30 @@ __device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup
   coord_base(r.X, r.dX, kbf, bix, fx);
   coord_base(r.Y, r.dY, kbf, biy, fy);
   coord_base(r.Z, r.dZ, kbf, biz, fz);
-  // padded indices of the lower taps are base + PAD + tap(fraction)
-  bix += PAD;
-  biy += PAD;
-  biz += PAD;
+  // Lower tap and weight per axis at fraction X (|X| < 2^22): t = M + X
+  // rounded down is M + floor(X), so floor(X) = bits(t) - bits(M) and the
+  // weight X - floor(X) in [0, 1) is exact.  The word of the lower taps has
+  // padded index (base + PAD + floor) per axis, i.e. bits(tz) pxy + bits(ty)
+  // px + bits(tx) + i_base in unsigned (mod 2^32) arithmetic, i_base folding
+  // the bases, the padding and bits(M).  Inside the box the taps stay in the
+  // padded grid; the one clamp keeps degenerate input in bounds.
+  const float M = 12582912.0f;  // 1.5 * 2^23
+  const unsigned BM = 0x4b400000u;
+  const unsigned i_base = ((unsigned)(biz + PAD) - BM) * pxy + ((unsigned)(biy + PAD) - BM) * px +
+                          ((unsigned)(bix + PAD) - BM);
+  const unsigned imax = (unsigned)(V.nz + 2 * PAD - 1) * pxy - px - 1u;
   float acc = 0.f, comp = 0.f;
   float j = (float)js;
 #pragma unroll 2
   for (int k = js; k <= je; ++k, j += 1.0f) {
     // j * (low part of d) stays below 1e-6 voxel for j < REBASE
-    int ix, iy, iz;
-    float ax, ay, az;
-    tap(fmaf(-j, dXh, fx), ix, ax);
-    tap(fmaf(-j, dYh, fy), iy, ay);
-    tap(fmaf(-j, dZh, fz), iz, az);
-    // inside the box the taps stay in the padded grid; the clamps only keep
-    // degenerate input in bounds
-    const unsigned xp = min((unsigned)(ix + bix), xmax);
-    const unsigned yp = min((unsigned)(iy + biy), ymax);
-    const unsigned zp = min((unsigned)(iz + biz), zmax);
-    const uint32_t* p0 = P + (size_t)zp * pxy + yp * px + xp;
+    const float X = fmaf(-j, dXh, fx), Y = fmaf(-j, dYh, fy), Z = fmaf(-j, dZh, fz);
+    const float tx = __fadd_rd(X, M), ty = __fadd_rd(Y, M), tz = __fadd_rd(Z, M);
+    const float ax = __fadd_rn(X, -__fadd_rn(tx, -M)), ay = __fadd_rn(Y, -__fadd_rn(ty, -M)),
+                az = __fadd_rn(Z, -__fadd_rn(tz, -M));
+    const unsigned i0 =
+        min(__float_as_uint(tz) * pxy + __float_as_uint(ty) * px + __float_as_uint(tx) + i_base, imax);
+    const uint32_t* p0 = P + i0;
     const uint32_t w00 = __ldg(p0), w10 = __ldg(p0 + px), w01 = __ldg(p0 + pxy), w11 = __ldg(p0 + pxy + px);
     const float e00 = lerp_pair<STORE>(w00, ax);
     const float e10 = lerp_pair<STORE>(w10, ax);

@@ -26,6 +26,15 @@ inline float __fsqrt_rn(float a) { return std::sqrt(a); }
 inline float __frcp_rn(float a) { volatile float r = 1.0f / a; return r; }
 inline float rsqrtf(float a) { volatile float r = 1.0f / std::sqrt(a); return r; }
 inline int __float_as_int(float f) { int i; std::memcpy(&i, &f, 4); return i; }
+inline unsigned __float_as_uint(float f) { unsigned i; std::memcpy(&i, &f, 4); return i; }
+// bytes of (y:x) picked by the selector's nibbles, lowest result byte first
+inline unsigned __byte_perm(unsigned x, unsigned y, unsigned s)
+{
+  const unsigned long long v = ((unsigned long long)y << 32) | x;
+  unsigned r = 0;
+  for (int i = 0; i < 4; ++i) r |= (unsigned)((v >> (8 * ((s >> (4 * i)) & 7u))) & 0xffu) << (8 * i);
+  return r;
+}
 inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline int __float2int_rd(float f) { return (int)std::floor(f); }
 template <class T> inline T __ldg(const T* p) { return *p; }
