@@ -963,6 +963,15 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
       rw < 1 || rh < 1 || max_items < 1 || (coverage != ASC_SUM_TREE && coverage != ASC_SUM_FULL))
     return ASC_ERR_ARG;
   if (cf_model != 0) return ASC_ERR_ARG;  // the engine scores NCC; SAD runs through asc_hdist
+  Gate g(device_gate());
+  // set-up work runs on a private stream, so that creating an engine does not
+  // wait for other engines' work
+  cudaStream_t cs = nullptr;
+  if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) return ASC_ERR_CUDA;
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { cudaStreamDestroy(s); }
+  } cs_guard{cs};
   auto* e = new asc_engine_s();
   SceneDev& S = e->host;
   memset(&S, 0, sizeof S);
@@ -1009,7 +1018,7 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
         delete e;
         return ASC_ERR_NOMEM;
       }
-      build_occupancy(vh->dev, B.cutoff_raw[v], occ, nullptr);
+      build_occupancy(vh->dev, B.cutoff_raw[v], occ, cs);
       B.occ[v] = occ;
     }
   }
@@ -1040,15 +1049,15 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
   if (!err) err = e->alloc(e->p_tmp, npix);
   if (!err) err = e->alloc(e->p_bgr, npix);
   if (!err) err = e->alloc(e->p_res, 1);
-  if (!err) err = cudaMemcpy(e->dev, &S, sizeof S, cudaMemcpyHostToDevice);
-  if (!err) err = cudaMemset(e->b.C, 0, sizeof(Counters));
+  if (!err) err = cudaMemcpyAsync(e->dev, &S, sizeof S, cudaMemcpyHostToDevice, cs);
+  if (!err) err = cudaMemsetAsync(e->b.C, 0, sizeof(Counters), cs);
   if (err) {
     delete e;
     return cuda_status(err);
   }
   e->vdesc.assign(views, views + n_views);
   e->bdesc.assign(bones, bones + n_bones);
-  if (asc_fill(e->p_bg, npix, 1.0f, nullptr) || cudaDeviceSynchronize()) {
+  if (asc_fill(e->p_bg, npix, 1.0f, cs) || cudaStreamSynchronize(cs)) {
     delete e;
     return ASC_ERR_CUDA;
   }
@@ -1071,6 +1080,7 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
 ASC_API int asc_engine_destroy(asc_engine e)
 {
   if (!e) return ASC_ERR_ARG;
+  Gate g(device_gate());
   cudaDeviceSynchronize();
   delete e;
   return ASC_OK;
@@ -1080,6 +1090,7 @@ ASC_API int asc_engine_set_base_pose(asc_engine e, int bone, const double xyzypr
 {
   if (!e || !xyzypr || bone < 0 || bone >= e->n_bones) return ASC_ERR_ARG;
   set_base(e->host.bones[bone], xyzypr);
+  Gate g(device_gate());
   ASC_CUDA(cudaMemcpy(&e->dev->bones[bone].base, xyzypr, 6 * sizeof(double), cudaMemcpyHostToDevice));
   return ASC_OK;
 }
@@ -1092,6 +1103,7 @@ ASC_API int asc_engine_set_radiograph(asc_engine e, int view, asc_image rad)
   d.rad = image_data(rad, &d.rad_w, &d.rad_h, &bps);
   if (bps == 32) return ASC_ERR_ARG;
   d.rad_bps = bps;
+  Gate g(device_gate());
   ASC_CUDA(cudaMemcpy(&e->dev->views[view], &d, sizeof d, cudaMemcpyHostToDevice));
   return ASC_OK;
 }
@@ -1194,6 +1206,7 @@ ASC_API int asc_engine_pso(asc_engine e, int np, int n_iter, double w, double c1
   }
   // swarm state: allocated once per engine, sized for max_items particles
   if (!e->sw_buf) {
+    Gate g(device_gate());
     const size_t cap = (size_t)e->max_items, nbm = (size_t)e->n_bones;
     cudaError_t err = e->alloc(e->sw_buf, cap * 6 * 3 + cap + nbm * 6 + nbm);
     if (!err) err = e->alloc(e->sw_iter, 1);
@@ -1221,6 +1234,7 @@ ASC_API int asc_engine_pso(asc_engine e, int np, int n_iter, double w, double c1
       e->pso_exec = nullptr;
     }
     cudaGraph_t graph = nullptr;
+    Gate g(device_gate());
     err = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (!err) {
       k_pso_update<<<gb, tb, 0, s>>>(sw, nb, np, w, c1, c2, seed);

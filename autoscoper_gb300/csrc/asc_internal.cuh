@@ -8,6 +8,8 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "../../include/autoscoper_gb300.h"
 
 #define ASC_API extern "C" __attribute__((visibility("default")))
@@ -26,6 +28,15 @@ inline cudaStream_t S(void* s) { return (cudaStream_t)s; }
   } while (0)
 
 #define ASC_LAUNCH_CHECK() ASC_CUDA(cudaGetLastError())
+
+// Stream capture on one thread must not overlap a call on another thread that
+// waits for the whole device (cudaDeviceSynchronize, cudaFree, pinned host
+// allocation, synchronous copies): that wait would include the capturing
+// stream, which fails the call and invalidates the capture.  Captures and
+// every library call that allocates, frees or synchronizes the device hold
+// this process-wide lock.
+std::recursive_mutex& device_gate();
+using Gate = std::lock_guard<std::recursive_mutex>;
 
 }  // namespace asc
 

@@ -484,6 +484,12 @@ static double* g_means = nullptr;
 static unsigned* g_ticket = nullptr;
 static unsigned g_max_n = 0;
 
+std::recursive_mutex& device_gate()
+{
+  static std::recursive_mutex m;
+  return m;
+}
+
 static int ensure_scratch(unsigned n)
 {
   if (n <= g_max_n && g_part) return ASC_OK;
@@ -527,11 +533,13 @@ ASC_API int asc_set_option(int option, int value)
 ASC_API int asc_malloc(void** p, size_t bytes)
 {
   if (!p) return ASC_ERR_ARG;
+  Gate g(device_gate());
   ASC_CUDA(cudaMalloc(p, bytes ? bytes : 1));
   return ASC_OK;
 }
 ASC_API int asc_free(void* p)
 {
+  Gate g(device_gate());
   ASC_CUDA(cudaFree(p));
   return ASC_OK;
 }
@@ -558,6 +566,7 @@ ASC_API int asc_stream_sync(void* st)
 }
 ASC_API int asc_device_sync(void)
 {
+  Gate g(device_gate());
   ASC_CUDA(cudaDeviceSynchronize());
   return ASC_OK;
 }
@@ -603,11 +612,13 @@ ASC_API int asc_event_destroy(void* e)
 ASC_API int asc_host_alloc(void** p, size_t n)
 {
   if (!p) return ASC_ERR_ARG;
+  Gate g(device_gate());
   ASC_CUDA(cudaMallocHost(p, n ? n : 1));
   return ASC_OK;
 }
 ASC_API int asc_host_free(void* p)
 {
+  Gate g(device_gate());
   ASC_CUDA(cudaFreeHost(p));
   return ASC_OK;
 }
@@ -727,6 +738,7 @@ ASC_API int asc_volume_create(const void* data, int W, int H, int D, int bps, co
   pack_pairs(dims[0], dims[1], dims[2],
              [&](int x, int y, int z) { return (uint32_t)to_store(vals[(size_t)z * dxy + (size_t)y * dx + x], storage); },
              pairs.data());
+  Gate g(device_gate());
   cudaError_t e = cudaMalloc(&v->pairs, nwords * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMemcpy(v->pairs, pairs.data(), nwords * sizeof(uint32_t), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
@@ -760,6 +772,7 @@ ASC_API int asc_volume_destroy(asc_volume vol)
 {
   auto* v = (asc_volume_host*)vol;
   if (!v) return ASC_ERR_ARG;
+  Gate g(device_gate());
   cudaFree(v->pairs);
   if (v->occ) cudaFree(v->occ);
   delete v;
@@ -807,7 +820,10 @@ ASC_API int asc_raycast(asc_volume vol, const double imv[16], const float vp[4],
   const uint8_t* occ = nullptr;
   if (g_empty_skip) {
     const float cut = cutoff / v->dev.norm;
-    if (!v->occ) ASC_CUDA(cudaMalloc(&v->occ, occupancy_cells(v->dev)));
+    if (!v->occ) {
+      Gate g(device_gate());
+      ASC_CUDA(cudaMalloc(&v->occ, occupancy_cells(v->dev)));
+    }
     if (!(v->occ_cutoff == cut)) {
       build_occupancy(v->dev, cut, v->occ, S(stream));
       ASC_LAUNCH_CHECK();
@@ -829,6 +845,7 @@ ASC_API int asc_image_create(const void* data, int w, int h, int bps, asc_image*
   if (!data || !out || w <= 0 || h <= 0 || (bps != 8 && bps != 16 && bps != 32)) return ASC_ERR_ARG;
   auto* im = new asc_image_s{nullptr, w, h, bps};
   size_t bytes = (size_t)w * h * (bps / 8);
+  Gate g(device_gate());
   cudaError_t e = cudaMalloc(&im->data, bytes);
   if (e == cudaSuccess) e = cudaMemcpy(im->data, data, bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
@@ -850,6 +867,7 @@ ASC_API int asc_image_update(asc_image im, const void* data, void* st)
 ASC_API int asc_image_destroy(asc_image im)
 {
   if (!im) return ASC_ERR_ARG;
+  Gate g(device_gate());
   cudaFree(im->data);
   delete im;
   return ASC_OK;
@@ -956,6 +974,7 @@ ASC_API int asc_sharpen(const float* in, float* out, int w, int h, float radius,
 ASC_API int asc_ncc_init(unsigned max_n)
 {
   std::lock_guard<std::mutex> l(g_red_mu);
+  Gate g(device_gate());
   if (g_part) cudaFree(g_part);
   if (g_means) cudaFree(g_means);
   if (g_ticket) cudaFree(g_ticket);
@@ -1007,6 +1026,7 @@ static int host_result(int rc, double* dev, double* out, void* st)
     if (e == cudaSuccess) e = cudaStreamSynchronize(S(st));
     if (e != cudaSuccess) rc = cuda_status(e);
   }
+  Gate g(device_gate());
   cudaFree(dev);
   return rc;
 }
@@ -1016,7 +1036,10 @@ ASC_API int asc_ncc_host(const float* f, const float* g, const float* m, unsigne
 {
   if (!out) return ASC_ERR_ARG;
   double* dev = nullptr;
-  ASC_CUDA(cudaMalloc(&dev, sizeof(double)));
+  {
+    Gate g(device_gate());
+    ASC_CUDA(cudaMalloc(&dev, sizeof(double)));
+  }
   return host_result(asc_ncc(f, g, m, n, coverage, dev, st), dev, out, st);
 }
 
@@ -1025,6 +1048,9 @@ ASC_API int asc_hdist_host(const float* f, const float* g, const float* m, unsig
 {
   if (!out) return ASC_ERR_ARG;
   double* dev = nullptr;
-  ASC_CUDA(cudaMalloc(&dev, sizeof(double)));
+  {
+    Gate g(device_gate());
+    ASC_CUDA(cudaMalloc(&dev, sizeof(double)));
+  }
   return host_result(asc_hdist(f, g, m, n, coverage, dev, st), dev, out, st);
 }

@@ -226,7 +226,8 @@ class Server:
         wall = now()
         lat = np.array([j.latency for j in jobs if j.error is None])
         evals = sum(j.evals for j in jobs)
-        return {"jobs": len(jobs), "failed": sum(j.error is not None for j in jobs), "wall_s": wall,
+        errors = sorted({j.error for j in jobs if j.error is not None})
+        return {"jobs": len(jobs), "failed": sum(j.error is not None for j in jobs), "errors": errors, "wall_s": wall,
                 "pose_evals": evals, "pose_evals_per_s": evals / wall if wall > 0 else 0.0,
                 "p50_latency_s": float(np.percentile(lat, 50)) if len(lat) else None,
                 "p99_latency_s": float(np.percentile(lat, 99)) if len(lat) else None,
