@@ -455,16 +455,50 @@ def run_precision(args):
             "storage": out, "oracle_sample": int(args.oracle_sample), "data": "batched PSO workload, synthetic"}
 
 
+def run_roofline(args):
+    """The roofline batch alone: `--particles` candidates per bone of the
+    default workload at fixed random manipulators, evaluated `--reps` times
+    (the profiling case for ncu: one k_ray/k_view launch per evaluation, the
+    first after the targets are rendered).  Prints the per-launch work."""
+    import ctypes as C
+    from autoscoper_gb300 import _lib as L, api
+    L.load()
+    sc = make_scene()
+    vols = render_targets(sc)
+    nb, npart = 3, args.particles
+    eng = api.Engine(sc, max_items=nb * npart, volumes=vols)
+    L.call("asc_engine_profile", eng.handle, 1)
+    rng = np.random.default_rng(3)
+    bones = np.repeat(np.arange(nb), npart).astype(np.int32)
+    man = np.concatenate([rng.uniform(-5, 5, (nb * npart, 3)), rng.uniform(-5, 5, (nb * npart, 3))], 1)
+    ms = []
+    for _ in range(args.reps):
+        eng.eval(bones, man)
+        t3 = (C.c_float * 3)()
+        L.call("asc_engine_stats", eng.handle, t3, None, None)
+        ms.append(list(t3))
+    cnt = (C.c_ulonglong * 4)()
+    L.call("asc_engine_counters", eng.handle, cnt)
+    ms = np.array(ms)
+    return {"workload": "roofline batch", "items": nb * npart, "views": 2, "reps": args.reps,
+            "samples_per_launch": cnt[0], "pixels_per_launch": cnt[1], "marched_per_launch": cnt[2],
+            "lane_slots_per_launch": cnt[3], "setup_ms": float(ms[:, 0].mean()), "ray_ms": float(ms[:, 1].mean()),
+            "view_ms": float(ms[:, 2].mean())}
+
+
 if __name__ == "__main__":
-    if len(sys.argv) > 1 and sys.argv[1] in ("tracking", "serving", "precision"):
+    if len(sys.argv) > 1 and sys.argv[1] in ("tracking", "serving", "precision", "roofline"):
         ap = argparse.ArgumentParser()
         ap.add_argument("workload")
         ap.add_argument("--frames", type=int, default=20)
         ap.add_argument("--jobs", type=int, default=24)
         ap.add_argument("--rate", type=float, default=2.0, help="mean job arrivals per second")
         ap.add_argument("--oracle-sample", type=int, default=12)
+        ap.add_argument("--particles", type=int, default=100, help="roofline: candidates per bone")
+        ap.add_argument("--reps", type=int, default=3, help="roofline: evaluations")
         a = ap.parse_args()
-        fn = {"tracking": run_tracking, "serving": run_serving, "precision": run_precision}[a.workload]
+        fn = {"tracking": run_tracking, "serving": run_serving, "precision": run_precision,
+              "roofline": run_roofline}[a.workload]
         print(json.dumps(fn(a)), flush=True)
     else:
         main()
