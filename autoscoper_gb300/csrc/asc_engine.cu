@@ -8,7 +8,7 @@
 //                            (item, view) crop, with prefix sums;
 //   k_ray         persistent: 16x16-ray tiles pulled from an atomic queue,
 //                            DRRs written to a packed buffer;
-//   k_view        persistent: 64x64 output tiles pulled from a queue; each
+//   k_view        persistent: 48x48 output tiles pulled from a queue; each
 //                            stages DRR and radiograph regions with the chain's
 //                            halo in shared memory, runs both filter chains,
 //                            the masks and the NCC moments; the last tile of a
@@ -37,10 +37,10 @@ constexpr int MAX_VIEWS = 4;
 constexpr int MAX_BONES = 16;
 constexpr int MAX_FILTERS = 8;
 #ifndef ASC_VT
-#define ASC_VT 64
+#define ASC_VT 48
 #endif
 #ifndef ASC_VIEW_MINBLOCKS
-#define ASC_VIEW_MINBLOCKS 2
+#define ASC_VIEW_MINBLOCKS 3
 #endif
 constexpr int VT = ASC_VT;   // k_view output tile edge
 constexpr int VNT = 256;     // k_view threads per block

@@ -429,17 +429,26 @@ __device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup
   const unsigned imax = (unsigned)(V.nz + 2 * PAD - 1) * pxy - px - 1u;
   float acc = 0.f, comp = 0.f;
   float j = (float)js;
-#pragma unroll 2
-  for (int k = js; k <= je; ++k, j += 1.0f) {
-    // j * (low part of d) stays below 1e-6 voxel for j < REBASE
-    const float X = fmaf(-j, dXh, fx), Y = fmaf(-j, dYh, fy), Z = fmaf(-j, dZh, fz);
+  // the taps' word index and weights of sample j (j * the low part of d
+  // stays below 1e-6 voxel for j < REBASE)
+  auto locate = [&](float jj, float& ax, float& ay, float& az) {
+    const float X = fmaf(-jj, dXh, fx), Y = fmaf(-jj, dYh, fy), Z = fmaf(-jj, dZh, fz);
     const float tx = __fadd_rd(X, M), ty = __fadd_rd(Y, M), tz = __fadd_rd(Z, M);
-    const float ax = __fadd_rn(X, -__fadd_rn(tx, -M)), ay = __fadd_rn(Y, -__fadd_rn(ty, -M)),
-                az = __fadd_rn(Z, -__fadd_rn(tz, -M));
-    const unsigned i0 =
-        min(__float_as_uint(tz) * pxy + __float_as_uint(ty) * px + __float_as_uint(tx) + i_base, imax);
-    const uint32_t* p0 = P + i0;
-    const uint32_t w00 = __ldg(p0), w10 = __ldg(p0 + px), w01 = __ldg(p0 + pxy), w11 = __ldg(p0 + pxy + px);
+    ax = __fadd_rn(X, -__fadd_rn(tx, -M));
+    ay = __fadd_rn(Y, -__fadd_rn(ty, -M));
+    az = __fadd_rn(Z, -__fadd_rn(tz, -M));
+    return P + min(__float_as_uint(tz) * pxy + __float_as_uint(ty) * px + __float_as_uint(tx) + i_base, imax);
+  };
+  float ax, ay, az;
+  const uint32_t* p0 = locate(j, ax, ay, az);
+  uint32_t w00 = __ldg(p0), w10 = __ldg(p0 + px), w01 = __ldg(p0 + pxy), w11 = __ldg(p0 + pxy + px);
+  for (int k = js; k <= je; ++k) {
+    // the next sample's loads go out before this sample's arithmetic (after
+    // the last sample they re-read clamped, in-bounds words)
+    j += 1.0f;
+    float bx, by, bz;
+    const uint32_t* q = locate(j, bx, by, bz);
+    const uint32_t n00 = __ldg(q), n10 = __ldg(q + px), n01 = __ldg(q + pxy), n11 = __ldg(q + pxy + px);
     const float e00 = lerp_pair<STORE>(w00, ax);
     const float e10 = lerp_pair<STORE>(w10, ax);
     const float e01 = lerp_pair<STORE>(w01, ax);
@@ -453,6 +462,13 @@ __device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup
       comp = (tt - acc) - y;
       acc = tt;
     }
+    w00 = n00;
+    w10 = n10;
+    w01 = n01;
+    w11 = n11;
+    ax = bx;
+    ay = by;
+    az = bz;
   }
   return make_float2(acc, comp);
 }
