@@ -453,101 +453,222 @@ __device__ __forceinline__ float contrast_pow(float axy, float v, float e1, floa
   return exp2f(l);
 }
 
+// Calls f(ry, rx, nr) for column units: column rx of the band [y0, y1) x
+// [x0, x1), rows ry .. ry + nr - 1 (nr <= VR), consecutive threads taking
+// consecutive columns.  A unit reads a few rows past the band; those reads
+// stay inside the block's shared memory (VR rows of slack follow the
+// buffers) and their results are discarded.
+constexpr int VR = 4;
+template <class F>
+__device__ __forceinline__ void for_units(int y0, int y1, int x0, int x1, F&& f)
+{
+  const int bw = x1 - x0, gh = (y1 - y0 + VR - 1) / VR, n = bw * gh;
+  if (bw <= 0 || gh <= 0) return;
+  const int dq = VNT / bw, dr = VNT - dq * bw;
+  int q = (int)threadIdx.x / bw;
+  int c = (int)threadIdx.x - q * bw;
+  for (int i = threadIdx.x; i < n; i += VNT) {
+    const int ry = y0 + q * VR;
+    f(ry, x0 + c, min(VR, y1 - ry));
+    c += dr;
+    q += dq;
+    if (c >= bw) {
+      c -= bw;
+      ++q;
+    }
+  }
+}
+
+__device__ __forceinline__ float clamp01(float v) { return fminf(fmaxf(v, 0.f), 1.f); }
+
+// Gaussian (kind 3) or Sharpen (kind 4) with a K-tap kernel: the 1-D weights
+// in registers, a horizontal pass into `tmp`, then a vertical pass in column
+// units that reuse each loaded value for up to VR outputs.  Positions outside
+// the image hold 0 in every stage buffer, which is the reference's skipping
+// of out-of-image taps.
+template <bool IN, int K>
+__device__ void blur_stage(const FilterDev& f, const float* in, float* out, float* tmp, const Region& g, int lo, int hi)
+{
+  constexpr int R = K / 2;
+  const int E = g.E;
+  float w[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) w[k] = f.g[k];
+  for_band(lo - R, hi + R, lo, hi, [&](int ry, int rx) {
+    const float* p = in + ry * E + rx - R;
+    float sum = 0.f;
+#pragma unroll
+    for (int k = 0; k < K; ++k) sum = fmaf(w[k], p[k], sum);
+    tmp[ry * E + rx] = sum;
+  });
+  __syncthreads();
+  const bool gauss = f.kind == 3;
+  const float p1 = f.p1, p2 = f.p2;
+  for_units(lo, hi, lo, hi, [&](int ry, int rx, int nr) {
+    float col[K + VR - 1];
+    const float* p = tmp + (ry - R) * E + rx;
+#pragma unroll
+    for (int t = 0; t < K + VR - 1; ++t) col[t] = p[t * E];
+#pragma unroll
+    for (int t = 0; t < VR; ++t) {
+      if (t < nr) {
+        float r = 0.f;
+        if (IN || inside(g, ry + t, rx)) {
+          float blur = 0.f;
+#pragma unroll
+          for (int k = 0; k < K; ++k) blur = fmaf(w[k], col[t + k], blur);
+          if (gauss) {
+            r = clamp01(blur);
+          } else {
+            const float v = in[(ry + t) * E + rx];
+            r = fabsf(v - blur) > p2 ? clamp01(v + p1 * (v - blur)) : v;
+          }
+        }
+        out[(ry + t) * E + rx] = r;
+      }
+    }
+  });
+}
+
+// Any kernel size: per-element passes with the weights in shared memory.
+template <bool IN>
+__device__ void blur_stage_any(const FilterDev& f, const float* in, float* out, float* tmp, float* wsh,
+                               const Region& g, int lo, int hi)
+{
+  const int E = g.E, K = f.K, R = f.R;
+  const float p1 = f.p1, p2 = f.p2;
+  if (threadIdx.x < K) wsh[threadIdx.x] = f.g[threadIdx.x];
+  __syncthreads();
+  for_band(lo - R, hi + R, lo, hi, [&](int ry, int rx) {
+    const float* p = in + ry * E + rx - R;
+    float sum = 0.f;
+    for (int k = 0; k < K; ++k) sum = fmaf(wsh[k], p[k], sum);
+    tmp[ry * E + rx] = sum;
+  });
+  __syncthreads();
+  for_band(lo, hi, lo, hi, [&](int ry, int rx) {
+    float r = 0.f;
+    if (IN || inside(g, ry, rx)) {
+      const float* p = tmp + (ry - R) * E + rx;
+      float blur = 0.f;
+      for (int k = 0; k < K; ++k) blur = fmaf(wsh[k], p[k * E], blur);
+      if (f.kind == 3) {
+        r = clamp01(blur);
+      } else {
+        const float v = in[ry * E + rx];
+        r = fabsf(v - blur) > p2 ? clamp01(v + p1 * (v - blur)) : v;
+      }
+    }
+    out[ry * E + rx] = r;
+  });
+}
+
+// SobelFilter_kernels.cu:63-113 at one pixel from its 3 x 3 neighbourhood.
+__device__ __forceinline__ float sobel_px(float p00, float p01, float p02, float p10, float p11, float p12, float p20,
+                                          float p21, float p22, float scale, float blend)
+{
+  const float horz = p02 + 2 * p12 + p22 - p00 - 2 * p10 - p20;
+  const float vert = p00 + 2 * p01 + p02 - p20 - 2 * p21 - p22;
+  const float grad = sqrtf(horz * horz + vert * vert);
+  const float s = blend < 0.5f ? scale * grad + 2.0f * blend * p11 : 2.0f * (1.0f - blend) * scale * grad + p11;
+  return clamp01(s);
+}
+
 // Applies one filter from `in` to `out` over the square band
 // [lo, hi) x [lo, hi) of region coordinates; positions outside the image get
-// 0.  `tmp` holds the horizontal pass of a Gaussian/Sharpen blur, `wsh` its
-// 1-D weights.  IN: the region lies inside the image.
+// 0.  `tmp` holds the horizontal pass of a Gaussian/Sharpen blur, `wsh` the
+// 1-D weights of a blur of uncommon size.  IN: the region lies inside the
+// image.
 template <bool IN>
 __device__ void apply_stage(const FilterDev& f, const float* in, float* out, float* tmp, float* wsh, const Region& g,
                             int lo, int hi)
 {
   const int E = g.E;
-  const int kind = f.kind, K = f.K, R = f.R;
-  const float p0 = f.p0, p1 = f.p1, p2 = f.p2;
+  const int kind = f.kind, K = f.K;
+  const float p0 = f.p0, p1 = f.p1;
   if (kind == 3 || kind == 4) {
-    if (threadIdx.x < K) wsh[threadIdx.x] = f.g[threadIdx.x];
-    __syncthreads();
-    // horizontal pass over rows [lo - R, hi + R)
-    for_band(lo - R, hi + R, lo, hi, [&](int ry, int rx) {
-      const float* p = in + ry * E + rx - R;
-      float s = 0.f;
-      for (int k = 0; k < K; ++k) s = fmaf(wsh[k], p[k], s);
-      tmp[ry * E + rx] = s;
-    });
-    __syncthreads();
-    for_band(lo, hi, lo, hi, [&](int ry, int rx) {
-      float r = 0.f;
-      if (IN || inside(g, ry, rx)) {
-        const float* p = tmp + (ry - R) * E + rx;
-        float blur = 0.f;
-        for (int k = 0; k < K; ++k) blur = fmaf(wsh[k], p[k * E], blur);
-        if (kind == 3) {
-          r = fminf(fmaxf(blur, 0.f), 1.f);
-        } else {
-          float v = in[ry * E + rx];
-          r = fabsf(v - blur) > p2 ? fminf(fmaxf(v + p1 * (v - blur), 0.f), 1.f) : v;
-        }
-      }
-      out[ry * E + rx] = r;
-    });
+    switch (K) {
+      case 3: blur_stage<IN, 3>(f, in, out, tmp, g, lo, hi); break;
+      case 5: blur_stage<IN, 5>(f, in, out, tmp, g, lo, hi); break;
+      case 7: blur_stage<IN, 7>(f, in, out, tmp, g, lo, hi); break;
+      case 9: blur_stage<IN, 9>(f, in, out, tmp, g, lo, hi); break;
+      case 11: blur_stage<IN, 11>(f, in, out, tmp, g, lo, hi); break;
+      case 13: blur_stage<IN, 13>(f, in, out, tmp, g, lo, hi); break;
+      default: blur_stage_any<IN>(f, in, out, tmp, wsh, g, lo, hi);
+    }
   } else if (kind == 1) {
-    for_band(lo, hi, lo, hi, [&](int ry, int rx) {
-      float r = 0.f;
-      if (IN || inside(g, ry, rx)) {
-        int xm = -1, xp = 1, ym = -E, yp = E;
-        if (!IN) {
-          int x = g.x0 + rx, y = g.y0 + ry;
-          xm = x > 0 ? -1 : 0;
-          xp = x < g.w - 1 ? 1 : 0;
-          ym = y > 0 ? -E : 0;
-          yp = y < g.h - 1 ? E : 0;
-        }
-        const float* c = in + ry * E + rx;
-        float p00 = c[ym + xm], p01 = c[ym], p02 = c[ym + xp];
-        float p10 = c[xm], p11 = c[0], p12 = c[xp];
-        float p20 = c[yp + xm], p21 = c[yp], p22 = c[yp + xp];
-        float horz = p02 + 2 * p12 + p22 - p00 - 2 * p10 - p20;
-        float vert = p00 + 2 * p01 + p02 - p20 - 2 * p21 - p22;
-        float grad = sqrtf(horz * horz + vert * vert);
-        float s = p1 < 0.5f ? p0 * grad + 2.0f * p1 * p11 : 2.0f * (1.0f - p1) * p0 * grad + p11;
-        r = fminf(fmaxf(s, 0.f), 1.f);
+    for_units(lo, hi, lo, hi, [&](int ry, int rx, int nr) {
+      float L[VR + 2], C[VR + 2], Rt[VR + 2];
+      const float* p = in + (ry - 1) * E + rx;
+#pragma unroll
+      for (int t = 0; t < VR + 2; ++t) {
+        L[t] = p[t * E - 1];
+        C[t] = p[t * E];
+        Rt[t] = p[t * E + 1];
       }
-      out[ry * E + rx] = r;
+#pragma unroll
+      for (int t = 0; t < VR; ++t) {
+        if (t < nr) {
+          float r = 0.f;
+          const int y = g.y0 + ry + t, x = g.x0 + rx;
+          if (IN || (x >= 0 && x < g.w && y >= 0 && y < g.h)) {
+            if (IN || (x > 0 && x < g.w - 1 && y > 0 && y < g.h - 1)) {
+              r = sobel_px(L[t], C[t], Rt[t], L[t + 1], C[t + 1], Rt[t + 1], L[t + 2], C[t + 2], Rt[t + 2], p0, p1);
+            } else {  // image border: neighbours outside the image repeat the edge
+              const int xm = x > 0 ? -1 : 0, xp = x < g.w - 1 ? 1 : 0, ym = y > 0 ? -E : 0, yp = y < g.h - 1 ? E : 0;
+              const float* c = in + (ry + t) * E + rx;
+              r = sobel_px(c[ym + xm], c[ym], c[ym + xp], c[xm], c[0], c[xp], c[yp + xm], c[yp], c[yp + xp], p0, p1);
+            }
+          }
+          out[(ry + t) * E + rx] = r;
+        }
+      }
+    });
+  } else if (kind == 0 && K == 3) {
+    // ContrastFilter_kernels.cu:62-96 with a 3 x 3 box: the mean over the
+    // window's in-image pixels (out-of-image positions hold 0, so the sum
+    // runs over the whole window and only the count depends on the border)
+    const float e1 = p0 - p1, e2 = p1;
+    for_units(lo, hi, lo, hi, [&](int ry, int rx, int nr) {
+      float rs[VR + 2];
+      const float* p = in + (ry - 1) * E + rx - 1;
+#pragma unroll
+      for (int t = 0; t < VR + 2; ++t) rs[t] = p[t * E] + p[t * E + 1] + p[t * E + 2];
+#pragma unroll
+      for (int t = 0; t < VR; ++t) {
+        if (t < nr) {
+          float r = 0.f;
+          const int y = g.y0 + ry + t, x = g.x0 + rx;
+          if (IN || (x >= 0 && x < g.w && y >= 0 && y < g.h)) {
+            float cnt = 9.0f;
+            if (!IN) cnt = (float)((min(y + 2, g.h) - max(y - 1, 0)) * (min(x + 2, g.w) - max(x - 1, 0)));
+            const float axy = (rs[t] + rs[t + 1] + rs[t + 2]) / cnt, v = in[(ry + t) * E + rx];
+            r = axy > 0.01f ? contrast_pow(axy, v, e1, e2) : 0.0f;
+          }
+          out[(ry + t) * E + rx] = r;
+        }
+      }
     });
   } else if (kind == 0) {
     const int size = K, h0 = size / 2, h1 = (size + 1) / 2;
     const float e1 = p0 - p1, e2 = p1;
-    if (IN) {
-      // every window is whole: size * size taps (the count the reference
-      // accumulates by adding 1.0f per tap is exact)
-      const float cnt = (float)(size * size);
-      for_band(lo, hi, lo, hi, [&](int ry, int rx) {
-        const float* c = in + (ry - h0) * E + rx - h0;
-        float s = 0.f;
-        for (int a = 0; a < size; ++a, c += E)
-          for (int q = 0; q < size; ++q) s += c[q];
-        float axy = s / cnt, v = in[ry * E + rx];
-        out[ry * E + rx] = axy > 0.01f ? contrast_pow(axy, v, e1, e2) : 0.0f;
-      });
-    } else {
-      for_band(lo, hi, lo, hi, [&](int ry, int rx) {
-        float r = 0.f;
-        if (inside(g, ry, rx)) {
-          int x = g.x0 + rx, y = g.y0 + ry;
-          int i0 = max(y - h0, 0), i1 = min(y + h1, g.h);
-          int j0 = max(x - h0, 0), j1 = min(x + h1, g.w);
-          float cnt = 0.f, s = 0.f;
-          for (int yy = i0; yy < i1; ++yy)
-            for (int xx = j0; xx < j1; ++xx) {
-              cnt += 1.0f;
-              s += in[(yy - g.y0) * E + (xx - g.x0)];
-            }
-          float axy = s / cnt, v = in[ry * E + rx];
-          r = axy > 0.01f ? contrast_pow(axy, v, e1, e2) : 0.0f;
-        }
-        out[ry * E + rx] = r;
-      });
-    }
+    for_band(lo, hi, lo, hi, [&](int ry, int rx) {
+      float r = 0.f;
+      if (IN || inside(g, ry, rx)) {
+        const int x = g.x0 + rx, y = g.y0 + ry;
+        const int i0 = max(y - h0, 0), i1 = min(y + h1, g.h);
+        const int j0 = max(x - h0, 0), j1 = min(x + h1, g.w);
+        float cnt = 0.f, sum = 0.f;
+        for (int yy = i0; yy < i1; ++yy)
+          for (int xx = j0; xx < j1; ++xx) {
+            cnt += 1.0f;
+            sum += in[(yy - g.y0) * E + (xx - g.x0)];
+          }
+        const float axy = sum / cnt, v = in[ry * E + rx];
+        r = axy > 0.01f ? contrast_pow(axy, v, e1, e2) : 0.0f;
+      }
+      out[ry * E + rx] = r;
+    });
   }
   __syncthreads();
 }
@@ -992,7 +1113,7 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
   S.E = VT + 2 * hmax;
   // three E x E stage buffers and the final tile must fit one block's shared
   // memory (227 KB less the static arrays)
-  if ((3 * S.E * S.E + VT * VT) * sizeof(float) > 224 * 1024) {
+  if ((3 * S.E * S.E + VT * VT + (VR + 2) * S.E) * sizeof(float) > 224 * 1024) {
     delete e;
     return ASC_ERR_RANGE;
   }
@@ -1061,7 +1182,9 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
     delete e;
     return ASC_ERR_CUDA;
   }
-  e->smem = (size_t)(3 * S.E * S.E + VT * VT) * sizeof(float);
+  // three stage buffers, the final DRR tile and VR + 2 rows of slack for the
+  // column units' reads past a band
+  e->smem = (size_t)(3 * S.E * S.E + VT * VT + (VR + 2) * S.E) * sizeof(float);
   e->smem = std::max(e->smem, (size_t)256 * sizeof(Moments));
   int dev = 0;
   cudaGetDevice(&dev);
