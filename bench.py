@@ -389,8 +389,9 @@ def run_tracking(args):
 
 
 def run_serving(args):
-    """Poisson stream of mixed registration jobs: continuous batching (4 slots,
-    HBM budget 150 GB, subject volume cache) against the FIFO loop."""
+    """Poisson stream (`--rate` jobs/s, `--jobs` jobs) of mixed registration
+    jobs: continuous batching (4 slots, HBM budget 150 GB, subject volume
+    cache) against the FIFO loop."""
     from autoscoper_gb300 import _lib as L, api, serve
     L.load()
 
@@ -400,8 +401,9 @@ def run_serving(args):
         subjects = [f"subject{i}" for i in range(max(2, args.jobs // 2))]
         for i in range(args.jobs):
             t += rng.exponential(1.0 / args.rate)
-            out.append(serve.make_job(i, rng, subjects[int(rng.integers(len(subjects)))], t, frames=(1, 5),
-                                      particles=(32, 128), iterations=10, render_targets=api.render_targets))
+            out.append(serve.make_job(i, rng, subjects[int(rng.integers(len(subjects)))], t,
+                                      frames=(1, args.max_frames), particles=(32, 128), iterations=args.pso_iters,
+                                      render_targets=api.render_targets))
         return out
 
     res = {}
@@ -413,15 +415,18 @@ def run_serving(args):
     return {"workload": "serving", "metric": "sustained pose evals/s; p50/p99 job latency",
             "value": c["pose_evals_per_s"], "unit": "pose-evals/s", "rate_jobs_per_s": args.rate,
             "continuous": c, "fifo": f, "speedup_vs_fifo": c["pose_evals_per_s"] / max(f["pose_evals_per_s"], 1e-9),
-            "data": "synthetic mixed jobs: volumes 64^3-320^3 u16, viewports 256^2-1024^2, 1-4 bones, 1-3 views, "
-                    "1-5 frames, PSO 32-128 particles x 10 iterations"}
+            "data": f"synthetic mixed jobs: volumes 64^3-320^3 u16, viewports 256^2-1024^2, 1-4 bones, 1-3 views, "
+                    f"1-{args.max_frames} frames, PSO 32-128 particles x {args.pso_iters} iterations"}
 
 
 def run_precision(args):
     """Storage precision on the batched workload: u16, FP16 and BF16 volumes
-    (FP32 sampling, compensated FP32 partials, FP64 combine) against the FP64
-    oracle on a sample of candidates, with pose-evals/s per storage."""
-    from autoscoper_gb300 import _lib as L, api
+    (FP32 sampling, compensated FP32 partials, FP64 combine).  Per storage:
+    NCC error against the FP64 oracle on a sample of candidates, pose-evals/s
+    on the 300-candidate batch, and the final pose error of `--frames` seeded
+    registrations (start poses +-5 mm / +-5 deg, PSO 64 x 30 then Downhill
+    Simplex per frame) against the ground truth and against the u16 result."""
+    from autoscoper_gb300 import _lib as L, api, scene as S
     from oracle import oracle as O
     L.load()
     sc = make_scene()
@@ -434,7 +439,12 @@ def run_precision(args):
     sample = rng.choice(n, size=args.oracle_sample, replace=False)
     ref = {int(k): [1.0 - c for c in tr.track_frame(int(bones[k]), tr.compose(int(bones[k]), man[k]))]
            for k in sample}
-    out = {}
+    starts = []
+    srng = np.random.default_rng(21)
+    for _ in range(args.frames):
+        starts.append([S.perturb(t, srng, 5.0, 5.0) for t in sc.truth])
+    truth = np.array([np.asarray(t, np.float64) for t in sc.truth])
+    out, poses_u16 = {}, None
     for name, st in (("u16", L.ASC_STORE_U16), ("f16", L.ASC_STORE_F16), ("bf16", L.ASC_STORE_BF16)):
         eng = api.Engine(sc, max_items=n, storage=st)
         cost, vcost = eng.eval(bones, man)
@@ -447,12 +457,30 @@ def run_precision(args):
         for _ in range(3):
             eng.eval(bones, man)
         dt = (time.perf_counter() - t0) / 3
-        out[name] = {"ncc_rel_err_max": float(np.max(errs)), "ncc_rel_err_median": float(np.median(errs)),
-                     "ncc_abs_err_max": float(np.max(aerrs)), "ncc_abs_err_median": float(np.median(aerrs)),
-                     "ncc_abs_min": float(np.min(nccs)), "ncc_abs_median": float(np.median(nccs)),
-                     "pose_evals_per_s": n / dt}
-    return {"workload": "precision", "metric": "NCC relative error vs FP64 oracle per volume storage",
-            "storage": out, "oracle_sample": int(args.oracle_sample), "data": "batched PSO workload, synthetic"}
+        finals = []
+        for f, start in enumerate(starts):
+            for b, p in enumerate(start):
+                eng.set_base_pose(b, p)
+            poses, _, _ = eng.optimize_frame(method=0, n_particles=64, n_iter=30, seed=300 + f)
+            finals.append(poses)
+        finals = np.array(finals)  # frames x bones x 6
+        err = np.abs(finals - truth[None])
+        row = {"ncc_rel_err_max": float(np.max(errs)), "ncc_rel_err_median": float(np.median(errs)),
+               "ncc_abs_err_max": float(np.max(aerrs)), "ncc_abs_err_median": float(np.median(aerrs)),
+               "ncc_abs_min": float(np.min(nccs)), "ncc_abs_median": float(np.median(nccs)),
+               "pose_evals_per_s": n / dt, "frames": len(starts),
+               "pose_err_vs_truth_mm": {"mean": float(err[..., :3].mean()), "max": float(err[..., :3].max())},
+               "pose_err_vs_truth_deg": {"mean": float(err[..., 3:].mean()), "max": float(err[..., 3:].max())}}
+        if poses_u16 is None:
+            poses_u16 = finals
+        else:
+            d = np.abs(finals - poses_u16)
+            row["pose_diff_vs_u16_mm_max"] = float(d[..., :3].max())
+            row["pose_diff_vs_u16_deg_max"] = float(d[..., 3:].max())
+        out[name] = row
+    return {"workload": "precision", "metric": "NCC error vs FP64 oracle and final pose error per volume storage",
+            "storage": out, "oracle_sample": int(args.oracle_sample),
+            "data": "batched PSO workload (3 bones, 2 views 1024^2, chain filters), synthetic"}
 
 
 def run_roofline(args):
@@ -494,6 +522,8 @@ if __name__ == "__main__":
         ap.add_argument("--jobs", type=int, default=24)
         ap.add_argument("--rate", type=float, default=2.0, help="mean job arrivals per second")
         ap.add_argument("--oracle-sample", type=int, default=12)
+        ap.add_argument("--max-frames", type=int, default=5, help="serving: frames per job drawn from 1..max")
+        ap.add_argument("--pso-iters", type=int, default=10, help="serving: PSO iterations per frame")
         ap.add_argument("--particles", type=int, default=100, help="roofline: candidates per bone")
         ap.add_argument("--reps", type=int, default=3, help="roofline: evaluations")
         a = ap.parse_args()
