@@ -745,81 +745,93 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
     const int rx0 = tx0 - eh, ry0 = ty0 - eh;
     const Region g{rx0, ry0, E, r.w, r.h, rx0 >= 0 && ry0 >= 0 && rx0 + E <= r.w && ry0 + E <= r.h};
     const float* drr = b.drr + r.pix;
-    // ---- DRR chain
+    // ---- DRR region; a region of zeros filters to zeros (every filter maps
+    // 0 to 0), so its tile masks out entirely and adds nothing to the moments
+    bool live;
     {
       const int lo = eh - V.h_drr, hi = eh + VT + V.h_drr;
+      bool nz = false;
       for_band(lo, hi, lo, hi, [&](int ry, int rx) {
-        bufs[0][ry * E + rx] =
+        const float d =
             (g.in || inside(g, ry, rx)) ? __ldg(drr + (long long)(g.y0 + ry) * r.w + g.x0 + rx) : 0.f;
+        bufs[0][ry * E + rx] = d;
+        nz |= d != 0.f;
       });
-      __syncthreads();
-      int res = run_chain(V.fdrr, V.n_drr, V.h_drr, bufs, wsh, g, eh);
-      for (int i = threadIdx.x; i < VT * VT; i += VNT) fdrr[i] = bufs[res][(eh + i / VT) * E + eh + i % VT];
-      __syncthreads();
+      live = __syncthreads_or(nz);
     }
-    // ---- radiograph crop and its chain
-    int rres;
-    {
-      const int lo = eh - V.h_rad, hi = eh + VT + V.h_rad;
-      for_band(lo, hi, lo, hi, [&](int ry, int rx) {
-        float val = 0.f, s, tt;
-        if ((g.in || inside(g, ry, rx)) && image_coords(V.ipf, r.vp, g.x0 + rx, g.y0 + ry, r.w, r.h, s, tt))
-          val = 1.0f - bilinear(V.rad, V.rad_bps, V.rad_w, V.rad_h, s, tt);
-        bufs[0][ry * E + rx] = val;
-      });
-      __syncthreads();
-      rres = run_chain(V.frad, V.n_rad, V.h_rad, bufs, wsh, g, eh);
-    }
-    // ---- masks and moments (Tracker.cpp:744-770), two passes over the
-    // tile: f = DRR * mask over fdrr, g = rad * mask over the chain result,
-    // the m > 0.5 flags in the free blur buffer
-    const unsigned n = (unsigned)r.w * (unsigned)r.h;
-    const bool tree = sc->coverage == ASC_SUM_TREE;
-    float* gres = bufs[rres];
-    float* flag = bufs[2];
-    float s[6] = {0, 0, 0, 0, 0, 0};
-    for (int i = threadIdx.x; i < VT * VT; i += VNT) {
-      const int ly = i / VT, lx = i % VT, x = tx0 + lx, y = ty0 + ly;
-      const int gi = (eh + ly) * E + eh + lx;
-      float f = 0.f, gm = 0.f, fl = 0.f;
-      if (x < r.w && y < r.h && (!tree || tree_keep((unsigned)(y * r.w + x), n))) {
-        float d = fdrr[i], gg = gres[gi];
-        float bg = 1.0f;
-        if (V.bg && V.bg_thr >= 0.f) {
-          float ss, tt;
-          bg = image_coords(V.ipf, r.vp, x, y, r.w, r.h, ss, tt)
-                 ? (V.bg_thr <= bilinear(V.bg, 32, V.bg_w, V.bg_h, ss, tt) ? 1.0f : 0.0f)
-                 : 0.0f;
-        }
-        float m = bg * (d != 0.0f ? 1.0f : 0.0f);
-        f = d * m;
-        gm = gg * m;
-        s[0] += m;
-        s[1] += f;
-        s[2] += gm;
-        if (m > 0.5f) {
-          fl = 1.f;
-          s[3] += 1.f;
-          s[4] += f;
-          s[5] += gm;
-        }
+    float s[6] = {0, 0, 0, 0, 0, 0}, c[3] = {0, 0, 0};
+    float cnt = 0.f, mf = 0.f, mg = 0.f;
+    if (live) {
+      // ---- DRR chain
+      {
+        int res = run_chain(V.fdrr, V.n_drr, V.h_drr, bufs, wsh, g, eh);
+        for (int i = threadIdx.x; i < VT * VT; i += VNT) fdrr[i] = bufs[res][(eh + i / VT) * E + eh + i % VT];
+        __syncthreads();
       }
-      fdrr[i] = f;
-      gres[gi] = gm;
-      flag[i] = fl;
-    }
-    bsum<6>(s, red);
-    const float cnt = s[3], mf = cnt > 0 ? s[4] / cnt : 0.f, mg = cnt > 0 ? s[5] / cnt : 0.f;
-    float c[3] = {0, 0, 0};
-    for (int i = threadIdx.x; i < VT * VT; i += VNT)
-      if (flag[i] != 0.f) {
-        const int ly = i / VT, lx = i % VT;
-        float a = fdrr[i] - mf, bb = gres[(eh + ly) * E + eh + lx] - mg;
-        c[0] = fmaf(a, a, c[0]);
-        c[1] = fmaf(bb, bb, c[1]);
-        c[2] = fmaf(a, bb, c[2]);
+      // ---- radiograph crop and its chain
+      int rres;
+      {
+        const int lo = eh - V.h_rad, hi = eh + VT + V.h_rad;
+        for_band(lo, hi, lo, hi, [&](int ry, int rx) {
+          float val = 0.f, s, tt;
+          if ((g.in || inside(g, ry, rx)) && image_coords(V.ipf, r.vp, g.x0 + rx, g.y0 + ry, r.w, r.h, s, tt))
+            val = 1.0f - bilinear(V.rad, V.rad_bps, V.rad_w, V.rad_h, s, tt);
+          bufs[0][ry * E + rx] = val;
+        });
+        __syncthreads();
+        rres = run_chain(V.frad, V.n_rad, V.h_rad, bufs, wsh, g, eh);
       }
-    bsum<3>(c, red);
+      // ---- masks and moments (Tracker.cpp:744-770), two passes over the
+      // tile: f = DRR * mask over fdrr, g = rad * mask over the chain result,
+      // the m > 0.5 flags in the free blur buffer
+      const unsigned n = (unsigned)r.w * (unsigned)r.h;
+      const bool tree = sc->coverage == ASC_SUM_TREE;
+      float* gres = bufs[rres];
+      float* flag = bufs[2];
+      for (int i = threadIdx.x; i < VT * VT; i += VNT) {
+        const int ly = i / VT, lx = i % VT, x = tx0 + lx, y = ty0 + ly;
+        const int gi = (eh + ly) * E + eh + lx;
+        float f = 0.f, gm = 0.f, fl = 0.f;
+        if (x < r.w && y < r.h && (!tree || tree_keep((unsigned)(y * r.w + x), n))) {
+          float d = fdrr[i], gg = gres[gi];
+          float bg = 1.0f;
+          if (V.bg && V.bg_thr >= 0.f) {
+            float ss, tt;
+            bg = image_coords(V.ipf, r.vp, x, y, r.w, r.h, ss, tt)
+                   ? (V.bg_thr <= bilinear(V.bg, 32, V.bg_w, V.bg_h, ss, tt) ? 1.0f : 0.0f)
+                   : 0.0f;
+          }
+          float m = bg * (d != 0.0f ? 1.0f : 0.0f);
+          f = d * m;
+          gm = gg * m;
+          s[0] += m;
+          s[1] += f;
+          s[2] += gm;
+          if (m > 0.5f) {
+            fl = 1.f;
+            s[3] += 1.f;
+            s[4] += f;
+            s[5] += gm;
+          }
+        }
+        fdrr[i] = f;
+        gres[gi] = gm;
+        flag[i] = fl;
+      }
+      bsum<6>(s, red);
+      cnt = s[3];
+      mf = cnt > 0 ? s[4] / cnt : 0.f;
+      mg = cnt > 0 ? s[5] / cnt : 0.f;
+      for (int i = threadIdx.x; i < VT * VT; i += VNT)
+        if (flag[i] != 0.f) {
+          const int ly = i / VT, lx = i % VT;
+          float a = fdrr[i] - mf, bb = gres[(eh + ly) * E + eh + lx] - mg;
+          c[0] = fmaf(a, a, c[0]);
+          c[1] = fmaf(bb, bb, c[1]);
+          c[2] = fmaf(a, bb, c[2]);
+        }
+      bsum<3>(c, red);
+    }  // live
     if (threadIdx.x == 0) {
       Moments p = {s[0], s[1], s[2], cnt, mf, mg, c[0], c[1], c[2]};
       b.part[tile] = p;

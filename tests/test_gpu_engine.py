@@ -89,6 +89,25 @@ def test_engine_batch_is_order_independent(scene):
     assert np.array_equal(c1[:5], single)
 
 
+def test_engine_empty_space_skipping_changes_no_bit(scene):
+    """The occupied-box screen, the DDA walk and the block trimming skip only
+    samples that add exactly nothing: costs and DRRs with skipping on equal
+    those of the full march, bit for bit."""
+    sc, tr = scene
+    rng = np.random.default_rng(5)
+    bones, man = _cands(rng, 24, len(sc.volumes), spread=4.0)
+    try:
+        L.call("asc_set_option", L.ASC_OPT_EMPTY_SKIP, 0)
+        eng_full = api.Engine(sc, max_items=32)
+        full, vfull = eng_full.eval(bones, man)
+    finally:
+        L.call("asc_set_option", L.ASC_OPT_EMPTY_SKIP, 1)
+    eng = api.Engine(sc, max_items=32)
+    skip, vskip = eng.eval(bones, man)
+    assert np.array_equal(full, skip)
+    assert np.array_equal(vfull, vskip)
+
+
 def test_engine_golden_reference_values():
     """NCC of the reference's own outputs (tests/golden) vs the engine."""
     import golden_scene
