@@ -6,9 +6,9 @@
 namespace asc {
 
 // --------------------------------------------------------------------------
-// Device volume.  Voxels are stored "x-paired": the word for voxel x holds
+// Device volume.  Voxels are stored "x-paired": a word for voxel x holds
 // voxel x in its low half and voxel x+1 in its high half, so that one 32-bit
-// load fetches both x taps of a trilinear sample.  The grid is padded by PAD
+// word carries both x taps of a trilinear sample.  The grid is padded by PAD
 // voxels on every side with copies of the edge voxels, which is
 // clamp-to-edge addressing (cutil_create_tex_obj.h:18-23) built into the
 // layout: the taps of any sample inside the volume box need no per-sample
@@ -18,19 +18,29 @@ namespace asc {
 // normalized float that cudaReadModeNormalizedFloat would return.
 // --------------------------------------------------------------------------
 constexpr int PAD = 2;
+// Each voxel holds two words, the x-pairs of rows y and y+1 ("quads"), so
+// that one 8-byte load fetches four taps of a sample and a sample takes two
+// loads (ASC_QUADS=0 builds the one-word pair layout, four loads a sample).
+#ifndef ASC_QUADS
+#define ASC_QUADS 1
+#endif
+constexpr int WPV = ASC_QUADS ? 2 : 1;  // words per voxel
 
 struct DevVolume {
-  const uint32_t* pairs;  // (nz + 2 PAD) slices of (ny + 2 PAD) rows of (nx + 2 PAD) words
+  const uint32_t* pairs;  // (nz + 2 PAD) slices of (ny + 2 PAD) rows of (nx + 2 PAD) voxels
   int nx, ny, nz;         // voxels of the volume itself
-  int px, pxy;            // padded row and slice pitch in words
+  int px, pxy;            // padded row and slice pitch in voxels
   int storage;
   float norm;
 };
 
 inline size_t padded_words(int nx, int ny, int nz)
 {
-  return (size_t)(nx + 2 * PAD) * (ny + 2 * PAD) * (nz + 2 * PAD);
+  return (size_t)WPV * (nx + 2 * PAD) * (ny + 2 * PAD) * (nz + 2 * PAD);
 }
+
+// The x-pair word of padded voxel index i (its low half is voxel i itself).
+__device__ __forceinline__ uint32_t pair_word(const DevVolume& V, size_t i) { return V.pairs[WPV * i]; }
 
 // Fills the padded paired layout from stored 16-bit halves v(x, y, z) of an
 // nx x ny x nz volume (host side).
@@ -42,9 +52,12 @@ inline void pack_pairs(int nx, int ny, int nz, F v, uint32_t* out)
   for (int zp = 0; zp < pz; ++zp)
     for (int yp = 0; yp < py; ++yp)
       for (int xp = 0; xp < px; ++xp) {
-        const int z = cl(zp - PAD, nz), y = cl(yp - PAD, ny);
-        const uint32_t lo = v(cl(xp - PAD, nx), y, z), hi = v(cl(xp - PAD + 1, nx), y, z);
-        out[((size_t)zp * py + yp) * px + xp] = lo | (hi << 16);
+        const int z = cl(zp - PAD, nz), x0 = cl(xp - PAD, nx), x1 = cl(xp - PAD + 1, nx);
+        const size_t i = ((size_t)zp * py + yp) * px + xp;
+        for (int r = 0; r < WPV; ++r) {
+          const int y = cl(yp - PAD + r, ny);
+          out[WPV * i + r] = v(x0, y, z) | (v(x1, y, z) << 16);
+        }
       }
 }
 
@@ -426,10 +439,11 @@ __device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup
   const unsigned BM = 0x4b400000u;
   const unsigned i_base = ((unsigned)(biz + PAD) - BM) * pxy + ((unsigned)(biy + PAD) - BM) * px +
                           ((unsigned)(bix + PAD) - BM);
-  const unsigned imax = (unsigned)(V.nz + 2 * PAD - 1) * pxy - px - 1u;
+  const unsigned imax = ASC_QUADS ? (unsigned)(V.nz + 2 * PAD - 1) * pxy - 1u
+                                  : (unsigned)(V.nz + 2 * PAD - 1) * pxy - px - 1u;
   float acc = 0.f, comp = 0.f;
   float j = (float)js;
-  // the taps' word index and weights of sample j (j * the low part of d
+  // the taps' voxel index and weights of sample j (j * the low part of d
   // stays below 1e-6 voxel for j < REBASE)
   auto locate = [&](float jj, float& ax, float& ay, float& az) {
     const float X = fmaf(-jj, dXh, fx), Y = fmaf(-jj, dYh, fy), Z = fmaf(-jj, dZh, fz);
@@ -437,18 +451,35 @@ __device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup
     ax = __fadd_rn(X, -__fadd_rn(tx, -M));
     ay = __fadd_rn(Y, -__fadd_rn(ty, -M));
     az = __fadd_rn(Z, -__fadd_rn(tz, -M));
-    return P + min(__float_as_uint(tz) * pxy + __float_as_uint(ty) * px + __float_as_uint(tx) + i_base, imax);
+    return min(__float_as_uint(tz) * pxy + __float_as_uint(ty) * px + __float_as_uint(tx) + i_base, imax);
+  };
+  // the four x-pair words (rows y, y+1 of slices z, z+1) of voxel index i
+  auto fetch = [&](unsigned i, uint32_t& w00, uint32_t& w10, uint32_t& w01, uint32_t& w11) {
+#if ASC_QUADS
+    const uint2* Q = reinterpret_cast<const uint2*>(P);
+    const uint2 a = __ldg(Q + i), c = __ldg(Q + i + pxy);
+    w00 = a.x;
+    w10 = a.y;
+    w01 = c.x;
+    w11 = c.y;
+#else
+    const uint32_t* p0 = P + i;
+    w00 = __ldg(p0);
+    w10 = __ldg(p0 + px);
+    w01 = __ldg(p0 + pxy);
+    w11 = __ldg(p0 + pxy + px);
+#endif
   };
   float ax, ay, az;
-  const uint32_t* p0 = locate(j, ax, ay, az);
-  uint32_t w00 = __ldg(p0), w10 = __ldg(p0 + px), w01 = __ldg(p0 + pxy), w11 = __ldg(p0 + pxy + px);
+  uint32_t w00, w10, w01, w11;
+  fetch(locate(j, ax, ay, az), w00, w10, w01, w11);
   for (int k = js; k <= je; ++k) {
     // the next sample's loads go out before this sample's arithmetic (after
     // the last sample they re-read clamped, in-bounds words)
     j += 1.0f;
     float bx, by, bz;
-    const uint32_t* q = locate(j, bx, by, bz);
-    const uint32_t n00 = __ldg(q), n10 = __ldg(q + px), n01 = __ldg(q + pxy), n11 = __ldg(q + pxy + px);
+    uint32_t n00, n10, n01, n11;
+    fetch(locate(j, bx, by, bz), n00, n10, n01, n11);
     const float e00 = lerp_pair<STORE>(w00, ax);
     const float e10 = lerp_pair<STORE>(w10, ax);
     const float e01 = lerp_pair<STORE>(w01, ax);

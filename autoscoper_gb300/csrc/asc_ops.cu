@@ -405,7 +405,7 @@ __global__ void k_occupancy(DevVolume V, float cutoff_raw, uint8_t* __restrict__
     for (int y = max(cy * OCC + lo, 0); y < min(cy * OCC + hi, V.ny); ++y)
       for (int x = max(cx * OCC + lo, 0); x < min(cx * OCC + hi, V.nx); ++x) {
         float lo, hi;
-        unpack<STORE>(V.pairs[(size_t)(z + PAD) * V.pxy + (size_t)(y + PAD) * V.px + (x + PAD)], lo, hi);
+        unpack<STORE>(pair_word(V, (size_t)(z + PAD) * V.pxy + (size_t)(y + PAD) * V.px + (x + PAD)), lo, hi);
         mx = fmaxf(mx, lo);
       }
   occ[c] = mx > cutoff_raw ? 1 : 0;

@@ -55,14 +55,15 @@ class Job:
         return self.finish - self.arrival
 
 
-PAD = 2  # edge voxels the device layout adds on every side
+PAD = 2          # edge voxels the device layout adds on every side
+VOXEL_BYTES = 8  # two x-pair words (rows y and y+1) per padded voxel
 
 
 def volume_bytes(vol: S.Volume) -> int:
-    """Device bytes of a volume: padded x-paired words plus occupancy grids."""
+    """Device bytes of a volume: the padded voxel words plus occupancy grids."""
     D, H, W = vol.data.shape
     cells = ((W + 7) // 8) * ((H + 7) // 8) * ((D + 7) // 8)
-    return 4 * (W + 2 * PAD) * (H + 2 * PAD) * (D + 2 * PAD) + 4 * cells
+    return VOXEL_BYTES * (W + 2 * PAD) * (H + 2 * PAD) * (D + 2 * PAD) + 4 * cells
 
 
 def engine_bytes(scene: S.Scene, max_items: int) -> int:
@@ -107,7 +108,7 @@ class VolumeCache:
         freed = 0
         with self.lock:
             for s in [s for s, r in self.refs.items() if r == 0]:
-                freed += sum(4 * int(np.prod(np.asarray(v.dims) + 2 * PAD)) for v in self.entries[s])
+                freed += sum(VOXEL_BYTES * int(np.prod(np.asarray(v.dims) + 2 * PAD)) for v in self.entries[s])
                 del self.entries[s]
                 del self.refs[s]
         return freed

@@ -42,7 +42,7 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
           for (int y = std::max(cy * OCC - OCC_LO, 0); y < std::min(cy * OCC + OCC + OCC_HI, ny); ++y)
             for (int x = std::max(cx * OCC - OCC_LO, 0); x < std::min(cx * OCC + OCC + OCC_HI, nx); ++x) {
               float lo, hi;
-              uint32_t wd = pairs[(size_t)(z + PAD) * pxy + (size_t)(y + PAD) * px + (x + PAD)];
+              uint32_t wd = pair_word(V, (size_t)(z + PAD) * pxy + (size_t)(y + PAD) * px + (x + PAD));
               if (storage == ASC_STORE_BF16) unpack<ASC_STORE_BF16>(wd, lo, hi);
               else unpack<ASC_STORE_U16>(wd, lo, hi);
               mx = std::max(mx, lo);

@@ -39,6 +39,7 @@ inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); retu
 inline int __float2int_rd(float f) { return (int)std::floor(f); }
 template <class T> inline T __ldg(const T* p) { return *p; }
 struct float2 { float x, y; };
+struct uint2 { unsigned x, y; };
 inline float2 make_float2(float x, float y) { return {x, y}; }
 struct __half2_raw { unsigned short x, y; };
 struct __half2 { unsigned short x, y; };
