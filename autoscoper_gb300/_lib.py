@@ -28,6 +28,10 @@ class OptParams(C.Structure):
                 ("lo", f64), ("hi", f64), ("seed", C.c_uint64), ("offsets", f64 * 6), ("ftol", f64)]
 
 
+class TrackParams(C.Structure):
+    _fields_ = [("opt", OptParams), ("repeats", i32), ("guess", i32), ("dframe", i32), ("keyed", P(i32))]
+
+
 class FilterDesc(C.Structure):
     _fields_ = [("kind", i32), ("enabled", i32), ("p0", f32), ("p1", f32), ("p2", f32)]
 
@@ -107,6 +111,8 @@ SIGNATURES = {
     "asc_amoeba": (i32, [COST_FN, vp, P(f64), P(f64), i32, f64, P(i32)]),
     "asc_amoeba_batch": (i32, [BATCH_COST_FN, vp, i32, P(f64), P(f64), i32, f64, P(i32)]),
     "asc_engine_optimize_frame": (i32, [vp, P(OptParams), P(f64), P(f64), P(C.c_longlong), vp]),
+    "asc_keycurve_store": (i32, [P(f64), P(f64)]),
+    "asc_engine_track": (i32, [vp, i32, P(vp), P(TrackParams), P(f64), P(f64), P(C.c_longlong), vp]),
 }
 
 _LIB = None

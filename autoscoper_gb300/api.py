@@ -309,6 +309,26 @@ class Engine:
                cost.ctypes.data_as(C.POINTER(C.c_double)), C.byref(ev), None)
         return poses, cost, ev.value
 
+    def track(self, frames, poses, method=0, n_particles=64, n_iter=30, w=0.7298, c1=1.4962, c2=1.4962, lo=-6.0,
+              hi=6.0, seed=1, offsets=(0.1,) * 6, ftol=1e-3, repeats=1, guess=1, dframe=1, keyed=None):
+        """A sequence of Tracker::optimize calls (asc_engine_track).  frames:
+        per frame, one DeviceImage per view; poses: (n_frames, n_bones, 6) key
+        curve values (the first tracked frame's is the start; `keyed` marks
+        other frames that hold a key).  Returns (poses, costs, evals)."""
+        nf, nb = len(frames), len(self.scene.volumes)
+        rads = (C.c_void_p * (nf * self.n_views))(*[img.handle for fr in frames for img in fr])
+        kf = None if keyed is None else np.ascontiguousarray(keyed, dtype=np.int32)
+        p = L.TrackParams(L.OptParams(method, n_particles, n_iter, w, c1, c2, lo, hi, seed, (C.c_double * 6)(*offsets),
+                                      ftol), repeats, guess, dframe,
+                          None if kf is None else kf.ctypes.data_as(C.POINTER(C.c_int)))
+        out = np.ascontiguousarray(np.array(poses, dtype=np.float64).reshape(nf, nb, 6))
+        cost = np.zeros((nf, nb))
+        ev = C.c_longlong()
+        L.call("asc_engine_track", self.handle, nf, rads, C.byref(p), out.ctypes.data_as(C.POINTER(C.c_double)),
+               cost.ctypes.data_as(C.POINTER(C.c_double)), C.byref(ev), None)
+        self.rads = list(frames[-1] if dframe > 0 else frames[0])  # the views' radiographs now
+        return out, cost, ev.value
+
     def debug_layout(self, n):
         d, lay = C.c_void_p(), C.c_void_p()
         L.call("asc_engine_debug", self.handle, C.byref(d), C.byref(lay))

@@ -1509,18 +1509,16 @@ int engine_batch_cost(int n, const int* who, const double* x, double* y, void* c
   return ASC_OK;
 }
 
-// The pose after a manipulator, rounded to float as the reference's key
-// curves store it (Tracker.cpp:479-491, :558-571).
-void apply_manip(const BoneDev& B, const double* manip, double* out)
+// The pose base * V^-1 * manip * V as xyzypr (Tracker.cpp:479-483, :558-562).
+void compose_pose(const BoneDev& B, const double* base6, const double* manip, double* out)
 {
   double base[12], man[12], t1[12], t2[12];
-  frame_from_xyzypr(B.base, base);
+  frame_from_xyzypr(base6, base);
   frame_from_axis_angle(manip, man);
   frame_mul(base, B.pivot_inv, t1);
   frame_mul(t1, man, t2);
   frame_mul(t2, B.pivot, t1);
   frame_to_xyzypr(t1, out);
-  for (int i = 0; i < 6; ++i) out[i] = (double)(float)out[i];
 }
 
 }  // namespace
@@ -1539,12 +1537,18 @@ ASC_API int asc_engine_optimize_frame(asc_engine e, const asc_opt_params* p, dou
   EvalCtx ctx{e, s, 0};
   std::vector<int> bones(nb);
   for (int b = 0; b < nb; ++b) bones[b] = b;
+  // the frame's pose as read from the key curves (the engine's base poses)
+  std::vector<double> xyzypr(6 * nb);
+  for (int b = 0; b < nb; ++b)
+    for (int j = 0; j < 6; ++j) xyzypr[6 * b + j] = e->host.bones[b].base[j];
   // init_ncc = minimizationFunc(0) (Tracker.cpp:441-443)
   std::vector<double> zero(6 * nb, 0.0), init(nb), fin(nb);
   int rc = engine_batch_cost(nb, bones.data(), zero.data(), init.data(), &ctx);
   if (rc) return rc;
   if (p->method == 0) {
-    // PSO, then move the pose to the swarm's best (Tracker.cpp:445-491)
+    // PSO, then move the pose to the swarm's best: the key curves take the
+    // stored (rounded) pose, which the simplex evaluates around, while the
+    // final composition starts from the unrounded one (Tracker.cpp:445-491)
     std::vector<double> best(6 * nb), bc(nb);
     long long ev = 0;
     rc = asc_engine_pso(e, p->n_particles, p->n_iter, p->w, p->c1, p->c2, p->lo, p->hi, p->seed, best.data(), bc.data(),
@@ -1552,9 +1556,11 @@ ASC_API int asc_engine_optimize_frame(asc_engine e, const asc_opt_params* p, dou
     if (rc) return rc;
     ctx.evals += ev;
     for (int b = 0; b < nb; ++b) {
-      double np[6];
-      apply_manip(e->host.bones[b], best.data() + 6 * b, np);
-      rc = asc_engine_set_base_pose(e, b, np);
+      double np[6], st[6];
+      compose_pose(e->host.bones[b], xyzypr.data() + 6 * b, best.data() + 6 * b, np);
+      keycurve_store(np, st);
+      for (int j = 0; j < 6; ++j) xyzypr[6 * b + j] = np[j];
+      rc = asc_engine_set_base_pose(e, b, st);
       if (rc) return rc;
     }
   }
@@ -1579,16 +1585,75 @@ ASC_API int asc_engine_optimize_frame(asc_engine e, const asc_opt_params* p, dou
   rc = engine_batch_cost(nb, bones.data(), vert0.data(), fin.data(), &ctx);
   if (rc) return rc;
   for (int b = 0; b < nb; ++b) {
+    const bool take = p->method != 0 || fin[b] < init[b];
     double manip[6] = {0, 0, 0, 0, 0, 0};
-    if (p->method != 0 || fin[b] < init[b])
+    if (take)
       for (int j = 0; j < 6; ++j) manip[j] = vert0[6 * b + j];
-    double np[6];
-    apply_manip(e->host.bones[b], manip, np);
-    rc = asc_engine_set_base_pose(e, b, np);
+    double np[6], st[6];
+    compose_pose(e->host.bones[b], xyzypr.data() + 6 * b, manip, np);
+    keycurve_store(np, st);
+    rc = asc_engine_set_base_pose(e, b, st);
     if (rc) return rc;
-    for (int j = 0; j < 6; ++j) pose_out[6 * b + j] = np[j];
-    if (cost_out) cost_out[b] = (p->method != 0 || fin[b] < init[b]) ? fin[b] : init[b];
+    for (int j = 0; j < 6; ++j) pose_out[6 * b + j] = st[j];
+    if (cost_out) cost_out[b] = take ? fin[b] : init[b];
   }
   if (evals_out) *evals_out = ctx.evals;
+  return ASC_OK;
+}
+
+ASC_API int asc_keycurve_store(const double pose[6], double out[6])
+{
+  if (!pose || !out) return ASC_ERR_ARG;
+  keycurve_store(pose, out);
+  return ASC_OK;
+}
+
+ASC_API int asc_engine_track(asc_engine e, int n_frames, const asc_image* rads, const asc_track_params* tp,
+                             double* poses, double* costs, long long* evals_out, void* stream)
+{
+  if (!e || n_frames < 1 || !rads || !tp || !poses || tp->repeats < 1 || (tp->dframe != 1 && tp->dframe != -1) ||
+      tp->guess < 0 || tp->guess > 2)
+    return ASC_ERR_ARG;
+  const int nb = e->n_bones, nv = e->n_views, d = tp->dframe;
+  long long evals = 0;
+  for (int i = 0; i < n_frames; ++i) {
+    const int f = d > 0 ? i : n_frames - 1 - i;
+    double* pf = poses + (size_t)f * nb * 6;
+    for (int v = 0; v < nv; ++v) {
+      int rc = asc_engine_set_radiograph(e, v, rads[(size_t)f * nv + v]);
+      if (rc) return rc;
+    }
+    // initial guess (Tracker.cpp:388-426); i frames are already tracked in
+    // this direction.  Without a guess the frame starts from its key curve
+    // value: its own key, or for an unkeyed frame the last tracked frame's
+    // pose (a key curve holds its last key beyond it)
+    for (int b = 0; b < nb; ++b) {
+      const double* prev = poses + ((size_t)(f - d) * nb + b) * 6;
+      double g[6];
+      if (tp->guess == 2 && i > 1) {
+        double a[12], c[12], x[12];
+        frame_from_xyzypr(poses + ((size_t)(f - 2 * d) * nb + b) * 6, a);
+        frame_from_xyzypr(prev, c);
+        frame_linear_extrap(a, c, x);
+        frame_to_xyzypr(x, g);
+        keycurve_store(g, pf + 6 * b);
+      } else if (tp->guess == 1 && i > 0) {
+        keycurve_store(prev, pf + 6 * b);
+      } else if (i > 0 && !(tp->keyed && tp->keyed[f])) {
+        for (int j = 0; j < 6; ++j) pf[6 * b + j] = prev[j];
+      }
+    }
+    for (int r = 0; r < tp->repeats; ++r) {
+      for (int b = 0; b < nb; ++b) {
+        int rc = asc_engine_set_base_pose(e, b, pf + 6 * b);
+        if (rc) return rc;
+      }
+      long long ev = 0;
+      int rc = asc_engine_optimize_frame(e, &tp->opt, pf, costs ? costs + (size_t)f * nb : nullptr, &ev, stream);
+      if (rc) return rc;
+      evals += ev;
+    }
+  }
+  if (evals_out) *evals_out = evals;
   return ASC_OK;
 }

@@ -251,6 +251,51 @@ __host__ __device__ inline void frame_point(const double* f, const double* p, do
   q[0] = r0; q[1] = r1; q[2] = r2;
 }
 
+// CoordFrame::linear_extrap (CoordFrame.cpp:419-476): from a at frame f - 2d
+// and b at f - d, the pose at f: b's translation step doubled, and a rotated
+// by twice the angle (about the axis) of the rotation from a to b.
+inline void frame_linear_extrap(const double* a, const double* b, double* out)
+{
+  const double PI = 3.14159265358979323846, t = 2.0;
+  const double trans[3] = {t * (b[9] - a[9]), t * (b[10] - a[10]), t * (b[11] - a[11])};
+  double A[9];  // a's rotation applied to b's, as the reference's element order
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) A[3 * r + c] = b[c] * a[r] + b[3 + c] * a[3 + r] + b[6 + c] * a[6 + r];
+  const double ang = acos((A[0] + A[4] + A[8] - 1.0) / 2.0);
+  double axis[3] = {1.0, 0.0, 0.0};  // angle 0: any axis
+  if (ang > 0.0 && ang < PI) {
+    axis[0] = A[5] - A[7];
+    axis[1] = A[6] - A[2];
+    axis[2] = A[1] - A[3];
+  }
+  for (int i = 0; i < 12; ++i) out[i] = a[i];
+  frame_rotate(out, axis, t * 180.0 * ang / PI);
+  out[9] += trans[0];
+  out[10] += trans[1];
+  out[11] += trans[2];
+}
+
+// The pose a trial's key curves hold after Tracker::optimize stores v and
+// reads it back (Tracker.cpp:422-438): x, y, z as float; the rotation as a
+// float quaternion from (yaw, pitch, roll) (Quaternion.hpp:80-94) read back
+// as Euler angles (Quaternion.hpp:220-243), in float math as there.
+inline void keycurve_store(const double* v, double* out)
+{
+  const float pi = (float)3.14159265358979323846;
+  const float yaw = (float)v[3], pitch = (float)v[4], roll = (float)v[5];
+  const float cr = cosf(roll * pi / 360.0f), sr = sinf(roll * pi / 360.0f);
+  const float cp = cosf(pitch * pi / 360.0f), sp = sinf(pitch * pi / 360.0f);
+  const float cy = cosf(yaw * pi / 360.0f), sy = sinf(yaw * pi / 360.0f);
+  const float w = cr * cp * cy + sr * sp * sy, x = sr * cp * cy - cr * sp * sy;
+  const float y = cr * sp * cy + sr * cp * sy, z = cr * cp * sy - sr * sp * cy;
+  const float rx = atan2f(2.0f * (w * x + y * z), 1.0f - 2.0f * (x * x + y * y));
+  const float ry = 2.0f * atan2f(sqrtf(1.0f + 2.0f * (w * y - x * z)), sqrtf(1.0f - 2.0f * (w * y - x * z))) - pi / 2.0f;
+  const float rz = atan2f(2.0f * (w * z + x * y), 1.0f - 2.0f * (y * y + z * z));
+  const double o[6] = {(float)v[0], (float)v[1], (float)v[2], rz * (180.0f / pi), ry * (180.0f / pi),
+                       rx * (180.0f / pi)};
+  for (int i = 0; i < 6; ++i) out[i] = o[i];
+}
+
 // RayCaster::setInvModelView (RayCaster.cpp:88-114) applied to the inverse of
 // `modelview`: the 3x4 camera->volume matrix with the volume normalisation
 // folded in, rounded to float as the reference stores it.

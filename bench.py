@@ -370,17 +370,15 @@ def run_tracking(args):
     rng = np.random.default_rng(5)
     sc.poses = [S.perturb(traj[b][0], rng, 1.0, 1.0) for b in range(2)]
     eng = api.Engine(sc, max_items=2 * 64, volumes=vols, images=images[0])
-    errs, evals = [], 0
+    start = np.zeros((nf, 2, 6))
+    start[0] = [np.asarray(p, np.float64) for p in sc.poses]
     L.call("asc_device_sync")
     t0 = time.perf_counter()
-    for f in range(nf):
-        for vi in range(2):
-            eng.set_radiograph(vi, images[f][vi])
-        poses, cost, ev = eng.optimize_frame(method=0, n_particles=64, n_iter=30, lo=-3.0, hi=3.0, seed=100 + f)
-        evals += ev
-        errs.append([np.abs(poses[b] - traj[b][f]) for b in range(2)])
+    # Tracker::optimize frame after frame, each from the previous frame's pose
+    poses, cost, evals = eng.track(images, start, method=0, n_particles=64, n_iter=30, lo=-3.0, hi=3.0, seed=100,
+                                   guess=1, repeats=1)
     dt = time.perf_counter() - t0
-    e = np.array(errs)  # frames x bones x 6
+    e = np.abs(poses - np.stack([traj[b] for b in range(2)], 1))  # frames x bones x 6
     return {"workload": "sequence tracking", "metric": "frames/s (end to end, PSO 64x30 + simplex, 2 bones, 2 views)",
             "value": nf / dt, "unit": "frames/s", "frames": nf, "pose_evals": evals, "pose_evals_per_s": evals / dt,
             "mean_err_mm": float(e[:, :, :3].mean()), "max_err_mm": float(e[:, :, :3].max()),

@@ -298,6 +298,33 @@ typedef struct {
 int asc_engine_optimize_frame(asc_engine e, const asc_opt_params *params, double *pose_out, double *cost_out,
                               long long *evals_out, void *stream);
 
+/* The pose a trial's key curves hold after Tracker::optimize stores `pose`
+ * (xyzypr) and reads it back (Tracker.cpp:422-438, KeyCurve<float> and
+ * KeyCurve<Quatf>): x, y, z rounded to float, the rotation through a float
+ * quaternion.  Host arithmetic only. */
+int asc_keycurve_store(const double pose[6], double out[6]);
+
+/* A sequence of Tracker::optimize calls (Tracker.cpp:337-580), frames in
+ * order (dframe +1) or in reverse (dframe -1).  Per frame: the views take
+ * the frame's radiographs rads[frame * n_views + view]; the start pose is
+ * the previous tracked frame's pose stored anew (guess 1, from the second
+ * tracked frame on), the linear extrapolation of the two previous tracked
+ * frames (guess 2, from the third on), or else the frame's key-curve value:
+ * poses[frame] for the first frame and for frames marked in `keyed`, the
+ * previous tracked frame's pose for the others (a curve holds its last key
+ * beyond it); then `repeats` times asc_engine_optimize_frame from the
+ * frame's pose.  poses: n_frames x n_bones x 6 (in: the key-curve values;
+ * out: the tracked poses); costs (optional): n_frames x n_bones. */
+typedef struct {
+  asc_opt_params opt;
+  int repeats;        /* >= 1 */
+  int guess;          /* 0, 1 or 2 (Trial::guess) */
+  int dframe;         /* +1 or -1 */
+  const int *keyed;   /* n_frames flags: the frame holds a key (NULL: none but the first) */
+} asc_track_params;
+int asc_engine_track(asc_engine e, int n_frames, const asc_image *rads, const asc_track_params *params,
+                     double *poses, double *costs, long long *evals_out, void *stream);
+
 /* Reference-sequential PSO on the host (PSO.cpp:198-295, asynchronous gBest,
  * glibc rand() after srand(seed), omega 0.8 * 0.9^epoch, c1 = c2 = 1.5),
  * with a caller-supplied cost.  Used to reproduce reference trajectories. */

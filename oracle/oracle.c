@@ -157,6 +157,33 @@ ORC_EXPORT void orc_frame_linear_extrap(const double a[12], const double b[12], 
   memcpy(out, x3, sizeof x3);
 }
 
+/* A pose as Tracker::optimize stores it in the trial's key curves and reads
+ * it back (Tracker.cpp:422-438): x, y, z as float; the rotation as a float
+ * quaternion from (yaw, pitch, roll) (Quaternion.hpp:80-94), read back as
+ * Euler angles (Quaternion.hpp:220-243).  Float math throughout, as there. */
+ORC_EXPORT void orc_keycurve_store(const double in[6], double out[6])
+{
+  const float pi = (float)M_PI;
+  const float yaw = (float)in[3], pitch = (float)in[4], roll = (float)in[5];
+  const float cr = cosf(roll * pi / 360.0f), sr = sinf(roll * pi / 360.0f);
+  const float cp = cosf(pitch * pi / 360.0f), sp = sinf(pitch * pi / 360.0f);
+  const float cy = cosf(yaw * pi / 360.0f), sy = sinf(yaw * pi / 360.0f);
+  const float w = cr * cp * cy + sr * sp * sy;
+  const float x = sr * cp * cy - cr * sp * sy;
+  const float y = cr * sp * cy + sr * cp * sy;
+  const float z = cr * cp * sy - sr * sp * cy;
+  const float r_x = atan2f(2.0f * (w * x + y * z), 1.0f - 2.0f * (x * x + y * y));
+  const float sp2 = sqrtf(1.0f + 2.0f * (w * y - x * z)), cp2 = sqrtf(1.0f - 2.0f * (w * y - x * z));
+  const float r_y = 2.0f * atan2f(sp2, cp2) - pi / 2.0f;
+  const float r_z = atan2f(2.0f * (w * z + x * y), 1.0f - 2.0f * (y * y + z * z));
+  out[0] = (float)in[0];
+  out[1] = (float)in[1];
+  out[2] = (float)in[2];
+  out[3] = r_z * (180.0f / pi);
+  out[4] = r_y * (180.0f / pi);
+  out[5] = r_x * (180.0f / pi);
+}
+
 /* ------------------------------------------------------------------ */
 /* Camera (libautoscoper/src/Camera.cpp:424-484)                       */
 /* ------------------------------------------------------------------ */

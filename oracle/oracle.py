@@ -135,6 +135,14 @@ def frame_linear_extrap(a, b):
     return out
 
 
+def keycurve_store(v):
+    """The pose a trial's key curves hold after Tracker::optimize stores v
+    (float translation, rotation through a float quaternion)."""
+    out = np.zeros(6)
+    lib().orc_keycurve_store(_dp(_arr(v)), _dp(out))
+    return out
+
+
 def camera_viewport(cx, cy, fx, fy, W, H):
     out = np.zeros(4)
     lib().orc_camera_viewport(cx, cy, fx, fy, W, H, _dp(out))

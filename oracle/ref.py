@@ -26,11 +26,15 @@ COST_FN = C.CFUNCTYPE(C.c_double, _d, C.c_void_p)
 
 
 def build() -> bool:
-    """Builds libascref.so when the reference sources are present."""
-    if os.path.exists(SO):
+    """Builds libascref.so when the reference sources are present (again
+    when the harness or its recipe changed)."""
+    deps = [os.path.join(HERE, "build_ref.sh")] + [os.path.join(HERE, "ref_shim", f)
+                                                   for f in os.listdir(os.path.join(HERE, "ref_shim"))]
+    fresh = os.path.exists(SO) and all(os.path.getmtime(d) <= os.path.getmtime(SO) for d in deps)
+    if fresh:
         return True
     if not os.path.isdir(os.path.join(REFERENCE_ROOT, "libautoscoper")):
-        return False
+        return os.path.exists(SO)
     subprocess.run([os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT], check=True,
                    stdout=subprocess.DEVNULL)
     return os.path.exists(SO)

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "CoordFrame.hpp"
+#include "Quaternion.hpp"
 #include "DownhillSimplex.hpp"
 #include "PSO.hpp"
 #include "Volume.hpp"
@@ -51,6 +52,17 @@ REF_EXPORT void ref_frame_linear_extrap(const double a[12], const double b[12], 
 {
   from_cf(to_cf(a).linear_extrap(to_cf(b)), o);
 }
+// A pose as Tracker::optimize writes it to the trial's key curves and reads
+// it back (Tracker.cpp:422-438): float x, y, z; the rotation through Quatf.
+REF_EXPORT void ref_keycurve_store(const double in[6], double out[6])
+{
+  const float x = (float)in[0], y = (float)in[1], z = (float)in[2];
+  const Quatf q(in[3], in[4], in[5]);
+  const Vec3f e = q.toEuler();
+  const double o[6] = {x, y, z, e.z, e.y, e.x};
+  for (int i = 0; i < 6; ++i) out[i] = o[i];
+}
+
 REF_EXPORT void ref_frame_row_matrix(const double a[12], double m[16]) { to_cf(a).to_matrix_row_order(m); }
 
 // ---- VolumeDescription ----

@@ -101,3 +101,16 @@ def test_batched_speculative_amoeba_follows_sequential_trajectories(lib):
         it = O.amoeba(lambda x, k=k: _quadratic_k(x, k), Pk, Yk, 1e-3)
         assert it == its[k]
         assert np.array_equal(Pk, Pb[k]) and np.array_equal(Yk, Yb[k])
+
+
+def test_keycurve_store_matches_oracle(lib):
+    """The pose storage of the trial's key curves (float translation, float
+    quaternion rotation) is bit-identical to the oracle's restatement, which
+    is pinned against the reference's Quaternion.hpp."""
+    rng = np.random.default_rng(9)
+    for _ in range(200):
+        v = np.concatenate([rng.uniform(-80, 80, 3), rng.uniform(-179, 179, 3)])
+        out = np.zeros(6)
+        _lib.call("asc_keycurve_store", v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                  out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        assert np.array_equal(out, O.keycurve_store(v)), (v, out, O.keycurve_store(v))

@@ -1,6 +1,8 @@
 """Tracker::optimize on the engine: the lock-step speculative simplex gives
-exactly the sequential AMOEBA's poses on the GPU cost, and PSO + simplex
-registers a perturbed frame back towards the ground truth."""
+exactly the sequential AMOEBA's poses on the GPU cost, PSO + simplex
+registers a perturbed frame back towards the ground truth, and a tracked
+sequence (initial guesses, repeats, key-curve storage) follows the
+reference's orchestration step for step."""
 import numpy as np
 import pytest
 
@@ -20,11 +22,26 @@ def _scene(seed):
     return sc
 
 
-def _apply(sc, b, manip):
-    base = G.from_xyzypr(np.asarray(sc.poses[b], np.float32).astype(np.float64))
+def _compose(sc, b, base, manip):
     V = sc.pivots[b]
-    f = G.mul(G.mul(G.mul(base, G.inverse(V)), G.from_axis_angle(manip)), V)
-    return G.to_xyzypr(f).astype(np.float32).astype(np.float64)
+    f = O.frame_mul(O.frame_mul(O.frame_mul(O.frame_from_xyzypr(base), O.frame_inverse(V)),
+                                O.frame_from_axis_angle(manip)), V)
+    return O.frame_to_xyzypr(f)
+
+
+def _apply(sc, b, manip):
+    base = np.asarray(sc.poses[b], np.float32).astype(np.float64)
+    return O.keycurve_store(_compose(sc, b, base, manip))
+
+
+def _simplex(eng, b, offsets=0.1, ftol=1e-3):
+    P = np.zeros((7, 6))
+    for i in range(1, 7):
+        P[i, i - 1] = offsets
+    cost = lambda x: float(eng.eval(np.array([b], np.int32), np.asarray(x).reshape(1, 6))[0][0])
+    Y = np.array([cost(p) for p in P])
+    Pf, _, _ = api.amoeba(cost, P, Y, ftol)
+    return Pf[0]
 
 
 def test_simplex_only_equals_sequential_amoeba():
@@ -59,3 +76,47 @@ def test_pso_plus_simplex_registers_frame():
         err_mm = np.abs(poses[b][:3] - sc.truth[b][:3]).max()
         start_mm = np.abs(np.asarray(sc.poses[b][:3], np.float64) - sc.truth[b][:3]).max()
         assert err_mm < start_mm
+
+
+def test_track_sequence_follows_reference_orchestration():
+    """Four frames of a linear motion, guess 2 (linear extrapolation from the
+    third frame on; before that the key curve's value, i.e. the previous
+    frame's pose), two repeats per frame, simplex only: asc_engine_track
+    against the orchestration of Tracker::optimize (Tracker.cpp:388-571)
+    written out on the host over the same engine's costs, with the oracle's
+    frame algebra and key-curve storage."""
+    sc = _scene(23)
+    tr = O.Tracker(sc)
+    from test_gpu_engine import make_targets
+    truth0 = [np.asarray(t, np.float64) for t in sc.truth]
+    step = np.array([0.3, -0.2, 0.15, 0.25, -0.15, 0.2])
+    frames = []
+    for f in range(4):
+        sc.truth = [t + f * step for t in truth0]
+        make_targets(sc, tr)
+        frames.append([v.radiograph.copy() for v in sc.views])
+    images = [[api.DeviceImage(r) for r in fr] for fr in frames]
+    nb = len(sc.volumes)
+    start = np.zeros((4, nb, 6))
+    start[0] = np.array([O.keycurve_store(p) for p in sc.poses])
+    eng = api.Engine(sc, max_items=64)
+    got, cost, evals = eng.track(images, start, method=1, guess=2, repeats=2)
+    # the reference's orchestration, step by step
+    ref_eng = api.Engine(sc, max_items=64)
+    want = start.copy()
+    for f in range(4):
+        for v in range(len(sc.views)):
+            ref_eng.set_radiograph(v, images[f][v])
+        for b in range(nb):
+            if f > 1:
+                x = O.frame_linear_extrap(O.frame_from_xyzypr(want[f - 2, b]), O.frame_from_xyzypr(want[f - 1, b]))
+                want[f, b] = O.keycurve_store(O.frame_to_xyzypr(x))
+            elif f > 0:
+                want[f, b] = want[f - 1, b]
+        for _ in range(2):
+            for b in range(nb):
+                ref_eng.set_base_pose(b, want[f, b])
+                manip = _simplex(ref_eng, b)
+                want[f, b] = O.keycurve_store(_compose(sc, b, want[f, b], manip))
+    assert evals > 0
+    assert np.abs(got - want).max() <= 2e-5, np.abs(got - want).max()

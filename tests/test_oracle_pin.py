@@ -27,6 +27,7 @@ def test_frames_bit_exact(ref_lib):
         assert np.array_equal(O.frame_inverse(f1), ref_lib.frame_op("ref_frame_inverse", f1))
         assert np.array_equal(O.frame_to_xyzypr(f1), ref_lib.frame_op("ref_frame_to_xyzypr", f1, n_out=6))
         assert np.array_equal(O.frame_row_matrix(f1), ref_lib.frame_op("ref_frame_row_matrix", f1, n_out=16))
+        assert np.array_equal(O.keycurve_store(x), ref_lib.frame_op("ref_keycurve_store", x, n_out=6))
         assert np.array_equal(O.frame_linear_extrap(f1, O.frame_mul(f1, f2)),
                               ref_lib.frame_op("ref_frame_linear_extrap", f1, O.frame_mul(f1, f2)))
         # the host-side numpy mirror agrees to rounding
