@@ -130,11 +130,14 @@ class Scene:
 # ---------------------------------------------------------------------------
 
 def phantom(shape, semi_axes=None, seed=0, noise=20.0, soft=200, cortex=1800, core=900, shell=3.0,
-            dtype=np.uint16) -> np.ndarray:
+            dtype=np.uint16, landmark=False) -> np.ndarray:
     """Bone phantom of shape (depth, height, width): soft tissue `soft`, an
     ellipsoidal cortical shell `cortex` of thickness `shell` voxels around a
     trabecular core `core`, plus Gaussian noise of sigma `noise` from
-    numpy PCG64(seed), rounded and clamped to the integer range."""
+    numpy PCG64(seed), rounded and clamped to the integer range.  The
+    ellipsoid is symmetric about an axis, so rotations about that axis do not
+    change its DRRs; `landmark` adds a dense sphere off the axes inside the
+    core, which makes every rotation observable."""
     D, H, W = shape
     if semi_axes is None:
         semi_axes = (0.31 * W, 0.31 * H, 0.31 * D)
@@ -146,6 +149,10 @@ def phantom(shape, semi_axes=None, seed=0, noise=20.0, soft=200, cortex=1800, co
     v = np.full(shape, float(soft))
     v[outer] = cortex
     v[inner] = core
+    if landmark:
+        r = 0.06 * min(D, H, W)
+        blob = (x - 0.12 * W) ** 2 + (y - 0.10 * H) ** 2 + (z - 0.08 * D) ** 2 <= r * r
+        v[blob & inner] = cortex
     rng = np.random.Generator(np.random.PCG64(seed))
     v += rng.normal(0.0, noise, size=shape)
     hi = np.iinfo(dtype).max
@@ -203,7 +210,7 @@ def config_filters(kind: str) -> List[Filter]:
 
 
 def make_scene(vol_shapes, voxel_mm, render, pitch_mm, filters="sobel", seed=0, bone_offsets=None,
-               rot_range=10.0, cutoff_frac=0.1) -> Scene:
+               rot_range=10.0, cutoff_frac=0.1, landmark=False) -> Scene:
     """Scene skeleton without radiographs (see `render_targets`).
 
     vol_shapes: list of (depth, height, width); render: (w, h) of both the
@@ -212,7 +219,8 @@ def make_scene(vol_shapes, voxel_mm, render, pitch_mm, filters="sobel", seed=0, 
     vols = []
     for i, shp in enumerate(vol_shapes):
         semi = (40, 25, 25) if tuple(shp) == (128, 128, 128) else None
-        vols.append(Volume(phantom(shp, semi, seed=seed + i), (voxel_mm,) * 3, subject=f"s{seed}_{i}"))
+        vols.append(Volume(phantom(shp, semi, seed=seed + i, landmark=landmark), (voxel_mm,) * 3,
+                           subject=f"s{seed}_{i}"))
     if bone_offsets is None:
         n = len(vols)
         bone_offsets = [(0.0, 0.0, 45.0 * (i - (n - 1) / 2.0)) for i in range(n)]
