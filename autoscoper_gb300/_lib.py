@@ -16,7 +16,7 @@ f64 = C.c_double
 P = C.POINTER
 
 ASC_OK = 0
-ASC_STORE_U16, ASC_STORE_F16, ASC_STORE_BF16 = 0, 1, 2
+ASC_STORE_U16, ASC_STORE_F16, ASC_STORE_BF16, ASC_STORE_F32 = 0, 1, 2, 3
 ASC_SUM_TREE, ASC_SUM_FULL = 0, 1
 ASC_OPT_EMPTY_SKIP = 1
 COST_FN = C.CFUNCTYPE(f64, P(f64), vp)

@@ -385,7 +385,9 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
       __syncthreads();
       const int nseg = s_nseg;
       // ---- march the segments, 32 at a time per warp
-      if (B.vol.storage == ASC_STORE_BF16)
+      if (B.vol.storage == ASC_STORE_F32)
+        march_segments<ASC_STORE_F32>(B.vol, s_rec, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
+      else if (B.vol.storage == ASC_STORE_BF16)
         march_segments<ASC_STORE_BF16>(B.vol, s_rec, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
       else if (B.vol.storage == ASC_STORE_F16)
         march_segments<ASC_STORE_F16>(B.vol, s_rec, s_ord, s_part, nseg, &s_grab, cut, marched, slots);

@@ -24,7 +24,11 @@ constexpr int PAD = 2;
 #ifndef ASC_QUADS
 #define ASC_QUADS 1
 #endif
-constexpr int WPV = ASC_QUADS ? 2 : 1;  // words per voxel
+constexpr int QROWS = ASC_QUADS ? 2 : 1;  // x-pairs (rows y, y+1) per voxel
+
+// 32-bit words per voxel: an x-pair is one word of two 16-bit halves, or two
+// FP32 words (ASC_STORE_F32).
+__host__ __device__ inline int voxel_words(int storage) { return (storage == ASC_STORE_F32 ? 2 : 1) * QROWS; }
 
 struct DevVolume {
   const uint32_t* pairs;  // (nz + 2 PAD) slices of (ny + 2 PAD) rows of (nx + 2 PAD) voxels
@@ -34,33 +38,34 @@ struct DevVolume {
   float norm;
 };
 
-inline size_t padded_words(int nx, int ny, int nz)
+inline size_t padded_words(int nx, int ny, int nz, int storage)
 {
-  return (size_t)WPV * (nx + 2 * PAD) * (ny + 2 * PAD) * (nz + 2 * PAD);
+  return (size_t)voxel_words(storage) * (nx + 2 * PAD) * (ny + 2 * PAD) * (nz + 2 * PAD);
 }
 
-// The x-pair word of padded voxel index i (its low half is voxel i itself).
-__device__ __forceinline__ uint32_t pair_word(const DevVolume& V, size_t i) { return V.pairs[WPV * i]; }
-
-// Fills the padded paired layout from stored 16-bit halves v(x, y, z) of an
-// nx x ny x nz volume (host side).
+// Fills the padded layout from stored values v(x, y, z) of an nx x ny x nz
+// volume (host side): 16-bit halves, or FP32 bits for ASC_STORE_F32.
 template <class F>
-inline void pack_pairs(int nx, int ny, int nz, F v, uint32_t* out)
+inline void pack_pairs(int nx, int ny, int nz, int storage, F v, uint32_t* out)
 {
-  const int px = nx + 2 * PAD, py = ny + 2 * PAD, pz = nz + 2 * PAD;
+  const int px = nx + 2 * PAD, py = ny + 2 * PAD, pz = nz + 2 * PAD, wpv = voxel_words(storage);
   auto cl = [](int i, int n) { return i < 0 ? 0 : (i > n - 1 ? n - 1 : i); };
   for (int zp = 0; zp < pz; ++zp)
     for (int yp = 0; yp < py; ++yp)
       for (int xp = 0; xp < px; ++xp) {
         const int z = cl(zp - PAD, nz), x0 = cl(xp - PAD, nx), x1 = cl(xp - PAD + 1, nx);
-        const size_t i = ((size_t)zp * py + yp) * px + xp;
-        for (int r = 0; r < WPV; ++r) {
+        uint32_t* o = out + (((size_t)zp * py + yp) * px + xp) * wpv;
+        for (int r = 0; r < QROWS; ++r) {
           const int y = cl(yp - PAD + r, ny);
-          out[WPV * i + r] = v(x0, y, z) | (v(x1, y, z) << 16);
+          if (storage == ASC_STORE_F32) {
+            o[2 * r] = v(x0, y, z);
+            o[2 * r + 1] = v(x1, y, z);
+          } else {
+            o[r] = v(x0, y, z) | (v(x1, y, z) << 16);
+          }
         }
       }
 }
-
 
 template <int STORE>
 __device__ __forceinline__ void unpack(uint32_t w, float& lo, float& hi)
@@ -99,6 +104,79 @@ __device__ __forceinline__ float lerp_pair(uint32_t w, float a)
     unpack<STORE>(w, lo, hi);
     return fmaf(a, hi - lo, lo);
   }
+}
+
+// Raw value of padded voxel i (the low half of its first x-pair).
+template <int STORE>
+__device__ __forceinline__ float voxel_value(const DevVolume& V, size_t i)
+{
+  const uint32_t w = V.pairs[(size_t)voxel_words(STORE) * i];
+  if constexpr (STORE == ASC_STORE_F32) {
+    return __uint_as_float(w);
+  } else {
+    float lo, hi;
+    unpack<STORE>(w, lo, hi);
+    return lo;
+  }
+}
+
+// The eight taps of a sample whose lower taps are voxel i, as its four
+// x-pairs (rows y, y+1 of slices z, z+1) in the storage's own form, and their
+// linear interpolation along x with weight a.
+template <int STORE>
+struct Taps {
+  uint32_t w[4];
+};
+template <>
+struct Taps<ASC_STORE_F32> {
+  float2 p[4];
+};
+
+template <int STORE>
+__device__ __forceinline__ Taps<STORE> fetch_taps(const uint32_t* __restrict__ P, unsigned i, unsigned px,
+                                                  unsigned pxy)
+{
+  Taps<STORE> t;
+  if constexpr (STORE == ASC_STORE_F32) {
+#if ASC_QUADS
+    const float4* Q = reinterpret_cast<const float4*>(P);
+    const float4 a = __ldg(Q + i), c = __ldg(Q + i + pxy);
+    t.p[0] = make_float2(a.x, a.y);
+    t.p[1] = make_float2(a.z, a.w);
+    t.p[2] = make_float2(c.x, c.y);
+    t.p[3] = make_float2(c.z, c.w);
+#else
+    const float2* Q = reinterpret_cast<const float2*>(P);
+    t.p[0] = __ldg(Q + i);
+    t.p[1] = __ldg(Q + i + px);
+    t.p[2] = __ldg(Q + i + pxy);
+    t.p[3] = __ldg(Q + i + pxy + px);
+#endif
+  } else {
+#if ASC_QUADS
+    const uint2* Q = reinterpret_cast<const uint2*>(P);
+    const uint2 a = __ldg(Q + i), c = __ldg(Q + i + pxy);
+    t.w[0] = a.x;
+    t.w[1] = a.y;
+    t.w[2] = c.x;
+    t.w[3] = c.y;
+#else
+    t.w[0] = __ldg(P + i);
+    t.w[1] = __ldg(P + i + px);
+    t.w[2] = __ldg(P + i + pxy);
+    t.w[3] = __ldg(P + i + pxy + px);
+#endif
+  }
+  return t;
+}
+
+template <int STORE>
+__device__ __forceinline__ float lerp_tap(const Taps<STORE>& t, int k, float a)
+{
+  if constexpr (STORE == ASC_STORE_F32)
+    return fmaf(a, t.p[k].y - t.p[k].x, t.p[k].x);
+  else
+    return lerp_pair<STORE>(t.w[k], a);
 }
 
 // Occupancy of 8x8x8-voxel cells for one cutoff: cell (cx, cy, cz) is 0 when
@@ -453,37 +531,18 @@ __device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup
     az = __fadd_rn(Z, -__fadd_rn(tz, -M));
     return min(__float_as_uint(tz) * pxy + __float_as_uint(ty) * px + __float_as_uint(tx) + i_base, imax);
   };
-  // the four x-pair words (rows y, y+1 of slices z, z+1) of voxel index i
-  auto fetch = [&](unsigned i, uint32_t& w00, uint32_t& w10, uint32_t& w01, uint32_t& w11) {
-#if ASC_QUADS
-    const uint2* Q = reinterpret_cast<const uint2*>(P);
-    const uint2 a = __ldg(Q + i), c = __ldg(Q + i + pxy);
-    w00 = a.x;
-    w10 = a.y;
-    w01 = c.x;
-    w11 = c.y;
-#else
-    const uint32_t* p0 = P + i;
-    w00 = __ldg(p0);
-    w10 = __ldg(p0 + px);
-    w01 = __ldg(p0 + pxy);
-    w11 = __ldg(p0 + pxy + px);
-#endif
-  };
   float ax, ay, az;
-  uint32_t w00, w10, w01, w11;
-  fetch(locate(j, ax, ay, az), w00, w10, w01, w11);
+  Taps<STORE> cur = fetch_taps<STORE>(P, locate(j, ax, ay, az), px, pxy);
   for (int k = js; k <= je; ++k) {
     // the next sample's loads go out before this sample's arithmetic (after
     // the last sample they re-read clamped, in-bounds words)
     j += 1.0f;
     float bx, by, bz;
-    uint32_t n00, n10, n01, n11;
-    fetch(locate(j, bx, by, bz), n00, n10, n01, n11);
-    const float e00 = lerp_pair<STORE>(w00, ax);
-    const float e10 = lerp_pair<STORE>(w10, ax);
-    const float e01 = lerp_pair<STORE>(w01, ax);
-    const float e11 = lerp_pair<STORE>(w11, ax);
+    const Taps<STORE> nxt = fetch_taps<STORE>(P, locate(j, bx, by, bz), px, pxy);
+    const float e00 = lerp_tap<STORE>(cur, 0, ax);
+    const float e10 = lerp_tap<STORE>(cur, 1, ax);
+    const float e01 = lerp_tap<STORE>(cur, 2, ax);
+    const float e11 = lerp_tap<STORE>(cur, 3, ax);
     const float f0 = fmaf(ay, e10 - e00, e00);
     const float f1 = fmaf(ay, e11 - e01, e01);
     const float s = fmaf(az, f1 - f0, f0);
@@ -493,10 +552,7 @@ __device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup
       comp = (tt - acc) - y;
       acc = tt;
     }
-    w00 = n00;
-    w10 = n10;
-    w01 = n01;
-    w11 = n11;
+    cur = nxt;
     ax = bx;
     ay = by;
     az = bz;

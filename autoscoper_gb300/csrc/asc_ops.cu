@@ -404,9 +404,7 @@ __global__ void k_occupancy(DevVolume V, float cutoff_raw, uint8_t* __restrict__
   for (int z = max(cz * OCC + lo, 0); z < min(cz * OCC + hi, V.nz); ++z)
     for (int y = max(cy * OCC + lo, 0); y < min(cy * OCC + hi, V.ny); ++y)
       for (int x = max(cx * OCC + lo, 0); x < min(cx * OCC + hi, V.nx); ++x) {
-        float lo, hi;
-        unpack<STORE>(pair_word(V, (size_t)(z + PAD) * V.pxy + (size_t)(y + PAD) * V.px + (x + PAD)), lo, hi);
-        mx = fmaxf(mx, lo);
+        mx = fmaxf(mx, voxel_value<STORE>(V, (size_t)(z + PAD) * V.pxy + (size_t)(y + PAD) * V.px + (x + PAD)));
       }
   occ[c] = mx > cutoff_raw ? 1 : 0;
 }
@@ -416,7 +414,9 @@ int g_empty_skip = 1;
 void build_occupancy(const DevVolume& V, float cutoff_raw, uint8_t* occ, cudaStream_t s)
 {
   int n = (int)occupancy_cells(V);
-  if (V.storage == ASC_STORE_BF16)
+  if (V.storage == ASC_STORE_F32)
+    k_occupancy<ASC_STORE_F32><<<(n + 127) / 128, 128, 0, s>>>(V, cutoff_raw, occ);
+  else if (V.storage == ASC_STORE_BF16)
     k_occupancy<ASC_STORE_BF16><<<(n + 127) / 128, 128, 0, s>>>(V, cutoff_raw, occ);
   else if (V.storage == ASC_STORE_F16)
     k_occupancy<ASC_STORE_F16><<<(n + 127) / 128, 128, 0, s>>>(V, cutoff_raw, occ);
@@ -680,10 +680,17 @@ static void describe(const T* data, int W, int H, int D, const int* flip, std::v
       }
 }
 
-static uint16_t to_store(unsigned v, int storage)
+// A voxel as stored: a 16-bit half (u16, IEEE half, bfloat16) or FP32 bits.
+static uint32_t to_store(unsigned v, int storage)
 {
   if (storage == ASC_STORE_F16) return __half_as_ushort(__float2half_rn((float)v));
   if (storage == ASC_STORE_BF16) return __bfloat16_as_ushort(__float2bfloat16_rn((float)v));
+  if (storage == ASC_STORE_F32) {
+    const float f = (float)v;
+    uint32_t b;
+    memcpy(&b, &f, 4);
+    return b;
+  }
   return (uint16_t)v;
 }
 
@@ -692,7 +699,7 @@ ASC_API int asc_volume_create(const void* data, int W, int H, int D, int bps, co
 {
   if (!data || !out || !scale || W <= 0 || H <= 0 || D <= 0) return ASC_ERR_ARG;
   if (bps != 8 && bps != 16) return ASC_ERR_ARG;
-  if (storage < ASC_STORE_U16 || storage > ASC_STORE_BF16) return ASC_ERR_ARG;
+  if (storage < ASC_STORE_U16 || storage > ASC_STORE_F32) return ASC_ERR_ARG;
   static const int noflip[3] = {0, 0, 0};
   if (!flip) flip = noflip;
   int mn[3], mx[3];
@@ -732,11 +739,11 @@ ASC_API int asc_volume_create(const void* data, int W, int H, int D, int bps, co
   v->inv_trans[2] = mn[2] / (float)dims[2];
   v->bps = bps;
   // x-paired words on the padded grid (see DevVolume)
-  const size_t nwords = padded_words(dims[0], dims[1], dims[2]);
+  const size_t nwords = padded_words(dims[0], dims[1], dims[2], storage);
   std::vector<uint32_t> pairs(nwords);
   const int dx = dims[0], dxy = dims[0] * dims[1];
-  pack_pairs(dims[0], dims[1], dims[2],
-             [&](int x, int y, int z) { return (uint32_t)to_store(vals[(size_t)z * dxy + (size_t)y * dx + x], storage); },
+  pack_pairs(dims[0], dims[1], dims[2], storage,
+             [&](int x, int y, int z) { return to_store(vals[(size_t)z * dxy + (size_t)y * dx + x], storage); },
              pairs.data());
   Gate g(device_gate());
   cudaError_t e = cudaMalloc(&v->pairs, nwords * sizeof(uint32_t));
@@ -793,7 +800,9 @@ int raycast_launch(const DevVolume& V, const uint8_t* occ, const float* m12, con
   df_split((double)vp[2] / (double)w, a.sx[0], a.sx[1]);
   df_split((double)vp[3] / (double)h, a.sy[0], a.sy[1]);
   dim3 grid((w + 15) / 16, (h + 15) / 16);
-  if (V.storage == ASC_STORE_BF16)
+  if (V.storage == ASC_STORE_F32)
+    k_raycast<ASC_STORE_F32><<<grid, 256, 0, s>>>(V, occ, a, out, w, h);
+  else if (V.storage == ASC_STORE_BF16)
     k_raycast<ASC_STORE_BF16><<<grid, 256, 0, s>>>(V, occ, a, out, w, h);
   else if (V.storage == ASC_STORE_F16)
     k_raycast<ASC_STORE_F16><<<grid, 256, 0, s>>>(V, occ, a, out, w, h);

@@ -501,7 +501,8 @@ def run_roofline(args):
     sc = make_scene()
     vols = render_targets(sc)
     nb, npart = 3, args.particles
-    eng = api.Engine(sc, max_items=nb * npart, volumes=vols)
+    st = {"u16": L.ASC_STORE_U16, "f16": L.ASC_STORE_F16, "bf16": L.ASC_STORE_BF16, "f32": L.ASC_STORE_F32}[args.storage]
+    eng = api.Engine(sc, max_items=nb * npart, volumes=vols if st == L.ASC_STORE_U16 else None, storage=st)
     L.call("asc_engine_profile", eng.handle, 1)
     rng = np.random.default_rng(3)
     bones = np.repeat(np.arange(nb), npart).astype(np.int32)
@@ -515,7 +516,7 @@ def run_roofline(args):
     cnt = (C.c_ulonglong * 4)()
     L.call("asc_engine_counters", eng.handle, cnt)
     ms = np.array(ms)
-    return {"workload": "roofline batch", "items": nb * npart, "views": 2, "reps": args.reps,
+    return {"workload": "roofline batch", "storage": args.storage, "items": nb * npart, "views": 2, "reps": args.reps,
             "samples_per_launch": cnt[0], "pixels_per_launch": cnt[1], "marched_per_launch": cnt[2],
             "lane_slots_per_launch": cnt[3], "setup_ms": float(ms[:, 0].mean()), "ray_ms": float(ms[:, 1].mean()),
             "view_ms": float(ms[:, 2].mean())}
@@ -533,6 +534,8 @@ if __name__ == "__main__":
         ap.add_argument("--pso-iters", type=int, default=10, help="serving: PSO iterations per frame")
         ap.add_argument("--particles", type=int, default=100, help="roofline: candidates per bone")
         ap.add_argument("--reps", type=int, default=3, help="roofline: evaluations")
+        ap.add_argument("--storage", default="u16", choices=["u16", "f16", "bf16", "f32"],
+                        help="roofline: volume storage")
         a = ap.parse_args()
         fn = {"tracking": run_tracking, "serving": run_serving, "precision": run_precision,
               "roofline": run_roofline}[a.workload]

@@ -36,6 +36,7 @@ extern "C" {
 #define ASC_STORE_U16 0   /* integer voxels as stored (u8/u16 input) */
 #define ASC_STORE_F16 1   /* voxels rounded to IEEE half */
 #define ASC_STORE_BF16 2  /* voxels rounded to bfloat16 */
+#define ASC_STORE_F32 3   /* voxels as FP32: twice the bytes, no unpacking in the march */
 
 /* NCC/SAD coverage: the reference's sum() (Ncc_kernels.cu:151-187) folds
  * each level's shared memory with s = T/2, T/4, ... and so drops partials

@@ -22,10 +22,16 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
                           const float* vp, float step, float intensity, float cutoff, float* out, int w, int h,
                           int* nsamples)
 {
-  if (storage != ASC_STORE_U16 && storage != ASC_STORE_BF16) return -1;
-  std::vector<uint32_t> pairs(padded_words(nx, ny, nz));
-  pack_pairs(nx, ny, nz, [&](int x, int y, int z) {
+  if (storage != ASC_STORE_U16 && storage != ASC_STORE_BF16 && storage != ASC_STORE_F32) return -1;
+  std::vector<uint32_t> pairs(padded_words(nx, ny, nz, storage));
+  pack_pairs(nx, ny, nz, storage, [&](int x, int y, int z) {
     unsigned v = vol[((size_t)z * ny + y) * nx + x];
+    if (storage == ASC_STORE_F32) {
+      const float f = (float)v;
+      uint32_t b;
+      std::memcpy(&b, &f, 4);
+      return b;
+    }
     return (uint32_t)(storage == ASC_STORE_BF16 ? to_bf16(v) : v);
   }, pairs.data());
   const int px = nx + 2 * PAD, pxy = px * (ny + 2 * PAD);
@@ -41,11 +47,10 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
         for (int z = std::max(cz * OCC - OCC_LO, 0); z < std::min(cz * OCC + OCC + OCC_HI, nz); ++z)
           for (int y = std::max(cy * OCC - OCC_LO, 0); y < std::min(cy * OCC + OCC + OCC_HI, ny); ++y)
             for (int x = std::max(cx * OCC - OCC_LO, 0); x < std::min(cx * OCC + OCC + OCC_HI, nx); ++x) {
-              float lo, hi;
-              uint32_t wd = pair_word(V, (size_t)(z + PAD) * pxy + (size_t)(y + PAD) * px + (x + PAD));
-              if (storage == ASC_STORE_BF16) unpack<ASC_STORE_BF16>(wd, lo, hi);
-              else unpack<ASC_STORE_U16>(wd, lo, hi);
-              mx = std::max(mx, lo);
+              const size_t i = (size_t)(z + PAD) * pxy + (size_t)(y + PAD) * px + (x + PAD);
+              mx = std::max(mx, storage == ASC_STORE_BF16 ? voxel_value<ASC_STORE_BF16>(V, i)
+                                : storage == ASC_STORE_F32 ? voxel_value<ASC_STORE_F32>(V, i)
+                                                           : voxel_value<ASC_STORE_U16>(V, i));
             }
         occ[((size_t)cz * by + cy) * bx + cx] = mx > cut ? 1 : 0;
       }
@@ -59,8 +64,9 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
       df_split((double)vp[3] / (double)h, sy.h, sy.l);
       if (ray_setup(m, vp, x, y, sx, sy, step, nx, ny, nz, r)) {
         const uint8_t* o = skip ? occ.data() : nullptr;
-        const float acc =
-            storage == ASC_STORE_BF16 ? march<ASC_STORE_BF16>(V, o, r, cut) : march<ASC_STORE_U16>(V, o, r, cut);
+        const float acc = storage == ASC_STORE_BF16  ? march<ASC_STORE_BF16>(V, o, r, cut)
+                          : storage == ASC_STORE_F32 ? march<ASC_STORE_F32>(V, o, r, cut)
+                                                     : march<ASC_STORE_U16>(V, o, r, cut);
         d = acc * (step * V.norm / intensity);
         n = r.K;
       }

@@ -40,6 +40,7 @@ inline int __float2int_rd(float f) { return (int)std::floor(f); }
 template <class T> inline T __ldg(const T* p) { return *p; }
 struct float2 { float x, y; };
 struct uint2 { unsigned x, y; };
+struct float4 { float x, y, z, w; };
 inline float2 make_float2(float x, float y) { return {x, y}; }
 struct __half2_raw { unsigned short x, y; };
 struct __half2 { unsigned short x, y; };

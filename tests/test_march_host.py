@@ -91,3 +91,17 @@ def test_host_march_bf16_matches_oracle_on_rounded_volume(hm, small):
     ref = O.raycast(v2, m, np.float32(vp).astype(np.float64), float(np.float32(rp.step)),
                     float(np.float32(rp.intensity)), float(np.float32(rp.cutoff)), w, h)
     assert np.abs(got - ref).max() < 1e-6
+
+
+def test_host_march_f32_storage_equals_u16(hm, small):
+    """FP32 voxels hold the same values as the u16 halves, and the march's
+    interpolation is the same arithmetic on them: identical DRRs."""
+    sc, tr = small
+    rng = np.random.default_rng(4)
+    pose = S.perturb(sc.truth[0], rng, 2.0, 10.0).astype(np.float64)
+    ok, m, vp, w, h = tr.view_setup(0, 1, pose)
+    rp = sc.ray[1][0]
+    a, na = run(hm, tr.vd[0], m, vp, rp, w, h, storage=0)
+    b, nb = run(hm, tr.vd[0], m, vp, rp, w, h, storage=3)
+    assert np.array_equal(na, nb)
+    assert np.array_equal(a, b)
