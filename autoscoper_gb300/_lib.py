@@ -112,6 +112,9 @@ SIGNATURES = {
     "asc_amoeba_batch": (i32, [BATCH_COST_FN, vp, i32, P(f64), P(f64), i32, f64, P(i32)]),
     "asc_engine_optimize_frame": (i32, [vp, P(OptParams), P(f64), P(f64), P(C.c_longlong), vp]),
     "asc_keycurve_store": (i32, [P(f64), P(f64)]),
+    "asc_background_from_frames": (i32, [P(vp), i32, vp, vp]),
+    "asc_engine_render_drr": (i32, [vp, i32, P(f64), P(f64), vp, vp]),
+    "asc_engine_image_data": (i32, [vp, i32, i32, P(f64), vp, vp, vp, P(i32), P(i32), vp]),
     "asc_engine_track": (i32, [vp, i32, P(vp), P(TrackParams), P(f64), P(f64), P(C.c_longlong), vp]),
 }
 

@@ -329,6 +329,33 @@ class Engine:
         self.rads = list(frames[-1] if dframe > 0 else frames[0])  # the views' radiographs now
         return out, cost, ev.value
 
+    def render_drr(self, view, poses, viewport=None):
+        """View::renderDrr: all bones at `poses` (n_bones x 6), merged and
+        filtered, over `viewport` (None: the whole image).  Returns (h, w)."""
+        cam = self.scene.views[view].camera
+        vp = np.array([-cam.viewport[2] / 2, -cam.viewport[3] / 2, cam.viewport[2], cam.viewport[3]]) \
+            if viewport is None else np.asarray(viewport, np.float64)
+        cvp = cam.viewport
+        w = min(int(vp[2] * self.scene.render_width / cvp[2]), self.scene.render_width)
+        h = min(int(vp[3] * self.scene.render_height / cvp[3]), self.scene.render_height)
+        out = DeviceArray((max(h, 1), max(w, 1)))
+        p = np.ascontiguousarray(poses, np.float64).reshape(-1)
+        vpa = np.ascontiguousarray(vp, np.float64)
+        L.call("asc_engine_render_drr", self.handle, view, p.ctypes.data_as(C.POINTER(C.c_double)),
+               vpa.ctypes.data_as(C.POINTER(C.c_double)), out.ptr, None)
+        return out.to_host()[:h, :w] if w > 0 and h > 0 else np.zeros((0, 0), np.float32)
+
+    def image_data(self, view, bone, pose):
+        """Tracker::getImageData: (rad, drr, mask) of the whole image at the
+        render size, as float arrays (to_u8 gives the reference's bytes)."""
+        h, w = self.scene.render_height, self.scene.render_width
+        rad, drr, mask = DeviceArray((h, w)), DeviceArray((h, w)), DeviceArray((h, w))
+        p = np.ascontiguousarray(pose, np.float64)
+        ww, hh = C.c_int(), C.c_int()
+        L.call("asc_engine_image_data", self.handle, view, bone, p.ctypes.data_as(C.POINTER(C.c_double)), rad.ptr,
+               drr.ptr, mask.ptr, C.byref(ww), C.byref(hh), None)
+        return rad.to_host(), drr.to_host(), mask.to_host()
+
     def debug_layout(self, n):
         d, lay = C.c_void_p(), C.c_void_p()
         L.call("asc_engine_debug", self.handle, C.byref(d), C.byref(lay))
@@ -381,3 +408,20 @@ def amoeba(cost, P, Y, ftol=1e-3):
     L.call("asc_amoeba", cb, None, P.ctypes.data_as(C.POINTER(C.c_double)),
            Y.ctypes.data_as(C.POINTER(C.c_double)), ndim, ftol, C.byref(it))
     return P, Y, it.value
+
+
+def to_u8(img):
+    """The bytes Tracker::getImageData returns for a float image
+    (Tracker.cpp:844-863): (unsigned char)(255 * v)."""
+    return (255.0 * np.asarray(img, np.float32)).astype(np.float32).astype(np.int64).astype(np.uint8)
+
+
+def background_from_frames(frames):
+    """Video::create_background_image: per pixel the largest normalized value
+    of the frames (arrays or DeviceImages of one size)."""
+    imgs = [f if isinstance(f, DeviceImage) else DeviceImage(f) for f in frames]
+    h, w = imgs[0].shape
+    out = DeviceArray((h, w))
+    arr = (C.c_void_p * len(imgs))(*[i.handle for i in imgs])
+    L.call("asc_background_from_frames", arr, len(imgs), out.ptr, None)
+    return out.to_host()

@@ -1409,6 +1409,18 @@ static int chain_plain(const asc_filter_desc* fl, int nf, float*& cur, float*& o
   return ASC_OK;
 }
 
+// One view of one bone at `xyzypr` over `vp`: the folded camera->volume
+// matrix (Tracker.cpp:603-612 with RayCaster::setInvModelView).
+static void view_matrix(const ViewDev& V, const BoneDev& B, const double* xyzypr, float m[12])
+{
+  double f[12], mv[12], imv[12], imv16[16];
+  frame_from_xyzypr(xyzypr, f);
+  frame_mul(V.cam_inv, f, mv);
+  frame_inverse(mv, imv);
+  frame_row_matrix(imv, imv16);
+  fold_matrix(imv16, B.inv_scale, B.inv_trans, m);
+}
+
 ASC_API int asc_engine_eval_plain(asc_engine e, int n, const int* bone, const double* manip, double* cost,
                                   double* view_cost, void* stream)
 {
@@ -1657,5 +1669,78 @@ ASC_API int asc_engine_track(asc_engine e, int n_frames, const asc_image* rads, 
     }
   }
   if (evals_out) *evals_out = evals;
+  return ASC_OK;
+}
+
+// ---------------------------------------------------------------- images
+ASC_API int asc_engine_render_drr(asc_engine e, int view, const double* poses, const double* viewport, float* out,
+                                  void* stream)
+{
+  if (!e || !poses || !out || view < 0 || view >= e->n_views) return ASC_ERR_ARG;
+  cudaStream_t s = S(stream);
+  const ViewDev& V = e->host.views[view];
+  const asc_view_desc& VD = e->vdesc[view];
+  const double full[4] = {-V.cvp[2] / 2, -V.cvp[3] / 2, V.cvp[2], V.cvp[3]};
+  const double* vp = viewport ? viewport : full;
+  // the render size of the viewport (Tracker.cpp:617-621), at most the buffer
+  const double fw = vp[2] * e->host.rw / V.cvp[2], fh = vp[3] * e->host.rh / V.cvp[3];
+  const int w = fw > 0 ? std::min((int)fw, e->host.rw) : 0, h = fh > 0 ? std::min((int)fh, e->host.rh) : 0;
+  if (w == 0 || h == 0) return ASC_OK;
+  const float vpf[4] = {(float)vp[0], (float)vp[1], (float)vp[2], (float)vp[3]};
+  // View::renderDrr (View.cpp:201-231): each bone's DRR merged (sum clamped
+  // to 1) into a zeroed buffer, then the view's DRR filters
+  ASC_CUDA(cudaMemsetAsync(e->p_mask, 0, (size_t)w * h * sizeof(float), s));
+  for (int b = 0; b < e->n_bones; ++b) {
+    const BoneDev& B = e->host.bones[b];
+    const asc_bone_desc& BD = e->bdesc[b];
+    float m[12];
+    view_matrix(V, B, poses + 6 * b, m);
+    int rc = raycast_launch(B.vol, g_empty_skip ? B.occ[view] : nullptr, m, vpf, BD.step[view], BD.intensity[view],
+                            BD.cutoff[view], e->p_drr, w, h, s);
+    if (!rc) rc = asc_merge(e->p_mask, e->p_drr, e->p_mask, w, h, s);
+    if (rc) return rc;
+  }
+  float *d = e->p_mask, *o = e->p_tmp;
+  int rc = chain_plain(VD.drr_filters, VD.n_drr_filters, d, o, w, h, s);
+  if (!rc) ASC_CUDA(cudaMemcpyAsync(out, d, (size_t)w * h * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  return rc;
+}
+
+ASC_API int asc_engine_image_data(asc_engine e, int view, int bone, const double pose[6], float* rad, float* drr,
+                                  float* mask, int* width, int* height, void* stream)
+{
+  if (!e || !pose || !rad || !drr || !mask || view < 0 || view >= e->n_views || bone < 0 || bone >= e->n_bones)
+    return ASC_ERR_ARG;
+  cudaStream_t s = S(stream);
+  const ViewDev& V = e->host.views[view];
+  const asc_view_desc& VD = e->vdesc[view];
+  const BoneDev& B = e->host.bones[bone];
+  const asc_bone_desc& BD = e->bdesc[bone];
+  // Tracker::getImageData (Tracker.cpp:865-925): the whole image, viewport
+  // (-w/2, -h/2, w, h) of the camera's, at the render size
+  const double vp[4] = {-V.cvp[2] / 2, -V.cvp[3] / 2, V.cvp[2], V.cvp[3]};
+  const int w = e->host.rw, h = e->host.rh;
+  const float vpf[4] = {(float)vp[0], (float)vp[1], (float)vp[2], (float)vp[3]};
+  float m[12];
+  view_matrix(V, B, pose, m);
+  int rc = raycast_launch(B.vol, g_empty_skip ? B.occ[view] : nullptr, m, vpf, BD.step[view], BD.intensity[view],
+                          BD.cutoff[view], e->p_drr, w, h, s);
+  float *d = e->p_drr, *o = e->p_tmp;
+  if (!rc) rc = chain_plain(VD.drr_filters, VD.n_drr_filters, d, o, w, h, s);
+  if (!rc) rc = asc_rad_render(VD.radiograph, V.ipf, vpf, e->p_rad, w, h, s);
+  float *r = e->p_rad, *ro = o;
+  if (!rc) rc = chain_plain(VD.rad_filters, VD.n_rad_filters, r, ro, w, h, s);
+  float* bgm = e->p_bg;
+  if (!rc && VD.background && VD.bg_threshold >= 0) {
+    bgm = e->p_bgr;
+    rc = asc_background_render(VD.background, V.ipf, vpf, VD.bg_threshold, bgm, w, h, s);
+  }
+  if (!rc) rc = asc_drr_background(d, mask, w, h, s);
+  if (!rc) rc = asc_multiply(bgm, mask, mask, w, h, s);
+  if (!rc) rc = asc_multiply(r, mask, rad, w, h, s);
+  if (!rc) rc = asc_multiply(d, mask, drr, w, h, s);
+  if (rc) return rc;
+  if (width) *width = w;
+  if (height) *height = h;
   return ASC_OK;
 }

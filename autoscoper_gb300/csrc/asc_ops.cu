@@ -882,6 +882,36 @@ ASC_API int asc_image_destroy(asc_image im)
   return ASC_OK;
 }
 
+// Video::create_background_image (Video.cpp:147-218): per pixel, the largest
+// normalized value over the frames (8, 16 or 32 bits per sample).
+__global__ void k_background_max(const void* __restrict__ img, int bps, size_t n, float* __restrict__ out)
+{
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    float v;
+    if (bps == 8)
+      v = (float)__ldg((const unsigned char*)img + i) / 255.0f;
+    else if (bps == 16)
+      v = (float)__ldg((const unsigned short*)img + i) / 65535.0f;
+    else
+      v = (float)__ldg((const unsigned*)img + i) / 4294967295.0f;
+    if (v > out[i]) out[i] = v;
+  }
+}
+
+ASC_API int asc_background_from_frames(const asc_image* frames, int n, float* out, void* st)
+{
+  if (!frames || !out || n < 2) return ASC_ERR_ARG;  // the reference wants two images at least
+  const int w = frames[0]->w, h = frames[0]->h;
+  for (int i = 0; i < n; ++i)
+    if (!frames[i] || frames[i]->w != w || frames[i]->h != h || frames[i]->bps == 32) return ASC_ERR_ARG;
+  const size_t px = (size_t)w * h;
+  ASC_CUDA(cudaMemsetAsync(out, 0, px * sizeof(float), S(st)));
+  const int blocks = (int)std::min<size_t>((px + 255) / 256, 4096);
+  for (int i = 0; i < n; ++i) k_background_max<<<blocks, 256, 0, S(st)>>>(frames[i]->data, frames[i]->bps, px, out);
+  ASC_LAUNCH_CHECK();
+  return ASC_OK;
+}
+
 namespace asc {
 const void* image_data(asc_image im, int* w, int* h, int* bps)
 {

@@ -142,6 +142,10 @@ int asc_merge(const float *a, const float *b, float *dst, int width, int height,
 int asc_composite(const float *a, const float *b, const float *c, const float *d, float *dst, int width, int height,
                   void *stream);
 int asc_fill(float *dst, size_t count, float value, void *stream);
+/* Video::create_background_image (Video.cpp:147-218): out (device, w*h
+ * floats) = per pixel the largest normalized value of n >= 2 frames (8 or
+ * 16 bits per sample, all of one size). */
+int asc_background_from_frames(const asc_image *frames, int n, float *out, void *stream);
 
 /* ---- filters ----
  * SobelFilter::apply (SobelFilter_kernels.cu:63-113), ContrastFilter::apply
@@ -298,6 +302,20 @@ typedef struct {
 } asc_opt_params;
 int asc_engine_optimize_frame(asc_engine e, const asc_opt_params *params, double *pose_out, double *cost_out,
                               long long *evals_out, void *stream);
+
+/* View::renderDrr (View.cpp:201-231) on an engine's view: the DRRs of all
+ * bones at poses (n_bones x 6 xyzypr) over `viewport` (NULL: the whole
+ * image, (-w/2, -h/2, w, h) of the camera viewport), summed and clamped to 1,
+ * then the view's DRR filters.  out: device floats of the render size
+ * (viewport size x render size / camera viewport, at most the engine's). */
+int asc_engine_render_drr(asc_engine e, int view, const double *poses, const double *viewport, float *out,
+                          void *stream);
+/* Tracker::getImageData (Tracker.cpp:865-925): bone `bone` at `pose` over
+ * the whole image at the engine's render size: the filtered radiograph, the
+ * filtered DRR and the mask (background x DRR mask), the first two masked.
+ * rad, drr, mask: device floats (render width x height, reported). */
+int asc_engine_image_data(asc_engine e, int view, int bone, const double pose[6], float *rad, float *drr,
+                          float *mask, int *width, int *height, void *stream);
 
 /* The pose a trial's key curves hold after Tracker::optimize stores `pose`
  * (xyzypr) and reads it back (Tracker.cpp:422-438, KeyCurve<float> and
