@@ -190,11 +190,23 @@ def pose_centered_at(vol: Volume, center_world, ypr) -> np.ndarray:
 
 def pivot_matrix(vol: Volume) -> np.ndarray:
     """Volume matrix after Tracker::load's "center pivot" translate by
-    VolumeDescription::transCenter (Tracker.cpp:286-290).  The phantoms have
-    no zero voxel, so the crop keeps the whole volume."""
-    D, H, W = vol.data.shape
+    VolumeDescription::transCenter (Tracker.cpp:286-290,
+    VolumeDescription.cpp:152-305): the centre of the box of non-zero voxels
+    of the flipped volume, scaled (the phantoms have no zero voxel, so theirs
+    is the whole volume)."""
+    d = vol.data
+    fx, fy, fz = (bool(f) for f in vol.flip)
+    d = d[::-1 if fz else 1, ::-1 if fy else 1, ::-1 if fx else 1]
+    mn, mx = [], []
+    for axis in (2, 1, 0):  # x, y, z
+        other = tuple(a for a in range(3) if a != axis)
+        idx = np.nonzero(np.any(d != 0, axis=other))[0]
+        if idx.size == 0:
+            raise ValueError("empty volume")
+        mn.append(int(idx[0]))
+        mx.append(int(idx[-1]))
     sx, sy, sz = (float(np.float32(s)) for s in vol.scale)
-    tc = [-sx * 0.5 * (0 + W - 1), -sy * 0.5 * (0 + H - 1), sz * 0.5 * (0 + D - 1)]
+    tc = [-sx * 0.5 * (mn[0] + mx[0]), -sy * 0.5 * (mn[1] + mx[1]), sz * 0.5 * (mn[2] + mx[2])]
     return G.translate(G.identity(), tc)
 
 
