@@ -19,13 +19,15 @@ ASC_OK = 0
 ASC_STORE_U16, ASC_STORE_F16, ASC_STORE_BF16, ASC_STORE_F32 = 0, 1, 2, 3
 ASC_SUM_TREE, ASC_SUM_FULL = 0, 1
 ASC_OPT_EMPTY_SKIP = 1
+ASC_CURVE_X, ASC_CURVE_Y, ASC_CURVE_Z, ASC_CURVE_ROT, ASC_CURVE_ALL = 1, 2, 4, 8, 15
 COST_FN = C.CFUNCTYPE(f64, P(f64), vp)
 BATCH_COST_FN = C.CFUNCTYPE(i32, i32, P(i32), P(f64), P(f64), vp)
 
 
 class OptParams(C.Structure):
     _fields_ = [("method", i32), ("n_particles", i32), ("n_iter", i32), ("w", f64), ("c1", f64), ("c2", f64),
-                ("lo", f64), ("hi", f64), ("seed", C.c_uint64), ("offsets", f64 * 6), ("ftol", f64)]
+                ("lo", f64), ("hi", f64), ("seed", C.c_uint64), ("offsets", f64 * 6), ("ftol", f64),
+                ("max_stall", i32)]
 
 
 class TrackParams(C.Structure):
@@ -107,11 +109,20 @@ SIGNATURES = {
     "asc_engine_counters": (i32, [vp, P(C.c_ulonglong)]),
     "asc_engine_pso": (i32, [vp, i32, i32, f64, f64, f64, f64, f64, C.c_uint64, P(f64), P(f64),
                              P(C.c_longlong), vp]),
+    "asc_engine_pso_stall": (i32, [vp, i32, i32, i32, f64, f64, f64, f64, f64, C.c_uint64, P(f64), P(f64),
+                                   P(C.c_longlong), P(i32), vp]),
     "asc_pso_sequential": (i32, [COST_FN, vp, i32, f32, f32, C.c_uint, C.c_uint, C.c_uint, P(f32), P(f32)]),
     "asc_amoeba": (i32, [COST_FN, vp, P(f64), P(f64), i32, f64, P(i32)]),
     "asc_amoeba_batch": (i32, [BATCH_COST_FN, vp, i32, P(f64), P(f64), i32, f64, P(i32)]),
     "asc_engine_optimize_frame": (i32, [vp, P(OptParams), P(f64), P(f64), P(C.c_longlong), vp]),
     "asc_keycurve_store": (i32, [P(f64), P(f64)]),
+    "asc_pose_curve_create": (i32, [P(vp)]),
+    "asc_pose_curve_destroy": (i32, [vp]),
+    "asc_pose_curve_clear": (i32, [vp]),
+    "asc_pose_curve_insert": (i32, [vp, i32, P(f64), i32]),
+    "asc_pose_curve_erase": (i32, [vp, i32, i32]),
+    "asc_pose_curve_keys": (i32, [vp, i32, P(i32)]),
+    "asc_pose_curve_eval": (i32, [vp, i32, P(f64)]),
     "asc_background_from_frames": (i32, [P(vp), i32, vp, vp]),
     "asc_engine_render_drr": (i32, [vp, i32, P(f64), P(f64), vp, vp]),
     "asc_engine_image_data": (i32, [vp, i32, i32, P(f64), vp, vp, vp, P(i32), P(i32), vp]),

@@ -286,22 +286,28 @@ class Engine:
     def eval_device(self, n, bone_dev: DeviceArray, manip_dev: DeviceArray, cost_dev: DeviceArray, stream=None):
         L.call("asc_engine_eval", self.handle, n, bone_dev.ptr, manip_dev.ptr, cost_dev.ptr, None, stream)
 
-    def pso(self, n_particles=100, n_iter=50, w=0.7298, c1=1.4962, c2=1.4962, lo=-6.0, hi=6.0, seed=1):
+    def pso(self, n_particles=100, n_iter=50, w=0.7298, c1=1.4962, c2=1.4962, lo=-6.0, hi=6.0, seed=1, max_stall=0):
+        """Batched PSO of every bone (asc_engine_pso_stall).  Returns (gBest
+        manipulators (n_bones, 6), their costs, evaluations); the iterations
+        run are left in `last_pso_iterations`."""
         nb = len(self.scene.volumes)
         best = np.zeros((nb, 6))
         cost = np.zeros(nb)
         ev = C.c_longlong()
-        L.call("asc_engine_pso", self.handle, n_particles, n_iter, w, c1, c2, lo, hi, seed,
+        its = C.c_int()
+        L.call("asc_engine_pso_stall", self.handle, n_particles, n_iter, max_stall, w, c1, c2, lo, hi, seed,
                best.ctypes.data_as(C.POINTER(C.c_double)), cost.ctypes.data_as(C.POINTER(C.c_double)),
-               C.byref(ev), None)
+               C.byref(ev), C.byref(its), None)
+        self.last_pso_iterations = its.value
         return best, cost, ev.value
 
     def optimize_frame(self, method=0, n_particles=64, n_iter=30, w=0.7298, c1=1.4962, c2=1.4962, lo=-6.0, hi=6.0,
-                       seed=1, offsets=(0.1,) * 6, ftol=1e-3):
+                       seed=1, offsets=(0.1,) * 6, ftol=1e-3, max_stall=0):
         """Tracker::optimize for one frame, all bones (asc_engine_optimize_frame).
         Returns (poses (n_bones, 6), costs (n_bones,), evaluations)."""
         nb = len(self.scene.volumes)
-        p = L.OptParams(method, n_particles, n_iter, w, c1, c2, lo, hi, seed, (C.c_double * 6)(*offsets), ftol)
+        p = L.OptParams(method, n_particles, n_iter, w, c1, c2, lo, hi, seed, (C.c_double * 6)(*offsets), ftol,
+                        max_stall)
         poses = np.zeros((nb, 6))
         cost = np.zeros(nb)
         ev = C.c_longlong()
@@ -310,7 +316,7 @@ class Engine:
         return poses, cost, ev.value
 
     def track(self, frames, poses, method=0, n_particles=64, n_iter=30, w=0.7298, c1=1.4962, c2=1.4962, lo=-6.0,
-              hi=6.0, seed=1, offsets=(0.1,) * 6, ftol=1e-3, repeats=1, guess=1, dframe=1, keyed=None):
+              hi=6.0, seed=1, offsets=(0.1,) * 6, ftol=1e-3, repeats=1, guess=1, dframe=1, keyed=None, max_stall=0):
         """A sequence of Tracker::optimize calls (asc_engine_track).  frames:
         per frame, one DeviceImage per view; poses: (n_frames, n_bones, 6) key
         curve values (the first tracked frame's is the start; `keyed` marks
@@ -319,7 +325,7 @@ class Engine:
         rads = (C.c_void_p * (nf * self.n_views))(*[img.handle for fr in frames for img in fr])
         kf = None if keyed is None else np.ascontiguousarray(keyed, dtype=np.int32)
         p = L.TrackParams(L.OptParams(method, n_particles, n_iter, w, c1, c2, lo, hi, seed, (C.c_double * 6)(*offsets),
-                                      ftol), repeats, guess, dframe,
+                                      ftol, max_stall), repeats, guess, dframe,
                           None if kf is None else kf.ctypes.data_as(C.POINTER(C.c_int)))
         out = np.ascontiguousarray(np.array(poses, dtype=np.float64).reshape(nf, nb, 6))
         cost = np.zeros((nf, nb))
@@ -408,6 +414,45 @@ def amoeba(cost, P, Y, ftol=1e-3):
     L.call("asc_amoeba", cb, None, P.ctypes.data_as(C.POINTER(C.c_double)),
            Y.ctypes.data_as(C.POINTER(C.c_double)), ndim, ftol, C.byref(it))
     return P, Y, it.value
+
+
+class PoseCurve:
+    """A volume's pose curves (asc_pose_curve: x, y, z KeyCurve<float> and
+    the rotation KeyCurve<Quatf>).  insert/erase take a mask of curves
+    (L.ASC_CURVE_X ... L.ASC_CURVE_ROT; all by default); eval reads the pose
+    at a frame as AutoscoperMainWindow::getPose does."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        L.call("asc_pose_curve_create", C.byref(h))
+        self.handle = h.value
+
+    def clear(self):
+        L.call("asc_pose_curve_clear", self.handle)
+
+    def insert(self, frame, xyzypr, mask=L.ASC_CURVE_ALL):
+        p = np.ascontiguousarray(xyzypr, np.float64)
+        L.call("asc_pose_curve_insert", self.handle, int(frame), p.ctypes.data_as(C.POINTER(C.c_double)), mask)
+
+    def erase(self, frame, mask=L.ASC_CURVE_ALL):
+        L.call("asc_pose_curve_erase", self.handle, int(frame), mask)
+
+    def keys(self, frame) -> int:
+        m = C.c_int()
+        L.call("asc_pose_curve_keys", self.handle, int(frame), C.byref(m))
+        return m.value
+
+    def eval(self, frame) -> np.ndarray:
+        out = np.zeros(6)
+        L.call("asc_pose_curve_eval", self.handle, int(frame), out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().asc_pose_curve_destroy(self.handle)
+        except Exception:
+            pass
 
 
 def to_u8(img):

@@ -76,6 +76,7 @@ struct BoneDev {
 
 struct SceneDev {
   int n_views, n_bones, rw, rh, coverage, E;
+  int cf_model;  // 0: 1 - NCC per view; 1: SAD ("hdist") per view
   ViewDev views[MAX_VIEWS];
   BoneDev bones[MAX_BONES];
 };
@@ -105,6 +106,9 @@ struct Bufs {
   int* foff;       // n_iv + 1 prefix of view tiles
   float* drr;
   Moments* part;   // per view tile
+  float2* fg;      // cf_model 1: masked DRR and radiograph per crop pixel
+  double2* hmean;  // cf_model 1: per-iv means of f and g
+  float* tsad;     // cf_model 1: per view tile SAD
   double* vcost;   // per iv
   unsigned* ivt;   // per-iv tile tickets
   unsigned* itt;   // per-item view tickets
@@ -184,7 +188,8 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
         df_split((double)r.vp[3] / (double)h, r.sy[0], r.sy[1]);
       }
       if (w == 0 || h == 0) {
-        vc = 1.0 - 1e5;  // degenerate NCC of an empty crop
+        // an empty crop: the degenerate NCC (1e5), or the SAD of no pixels
+        vc = sc->cf_model ? 0.0 : 1.0 - 1e5;
       } else {
         r.ok = 1;
         r.rtx = (r.w + RTX - 1) / RTX;
@@ -788,6 +793,7 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
       // the m > 0.5 flags in the free blur buffer
       const unsigned n = (unsigned)r.w * (unsigned)r.h;
       const bool tree = sc->coverage == ASC_SUM_TREE;
+      const bool sad = sc->cf_model != 0;
       float* gres = bufs[rres];
       float* flag = bufs[2];
       for (int i = threadIdx.x; i < VT * VT; i += VNT) {
@@ -819,12 +825,14 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
         fdrr[i] = f;
         gres[gi] = gm;
         flag[i] = fl;
+        // SAD needs the view's global means first: keep f and g for k_sad
+        if (sad && x < r.w && y < r.h) b.fg[r.pix + (long long)y * r.w + x] = make_float2(f, gm);
       }
       bsum<6>(s, red);
       cnt = s[3];
       mf = cnt > 0 ? s[4] / cnt : 0.f;
       mg = cnt > 0 ? s[5] / cnt : 0.f;
-      for (int i = threadIdx.x; i < VT * VT; i += VNT)
+      for (int i = threadIdx.x; i < VT * VT && !sad; i += VNT)
         if (flag[i] != 0.f) {
           const int ly = i / VT, lx = i % VT;
           float a = fdrr[i] - mf, bb = gres[(eh + ly) * E + eh + lx] - mg;
@@ -853,7 +861,13 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
       if (threadIdx.x < st) moments_merge(msh[threadIdx.x], msh[threadIdx.x + st]);
       __syncthreads();
     }
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && sc->cf_model) {
+      // HDist_kernels.cu:111-115: the means over the mask sum; k_sad takes
+      // the view from here and reuses its tile tickets
+      const Moments& m = msh[0];
+      b.hmean[k] = make_double2(m.sf / m.sm, m.sg / m.sm);
+      b.ivt[k] = 0;
+    } else if (threadIdx.x == 0) {
       double vc = 1.0 - moments_ncc(msh[0]);
       b.vcost[k] = vc;
       __threadfence();
@@ -863,6 +877,73 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
         finish_item(sc, b, item, cost);
         if (view_cost_out)
           for (int j = 0; j < nv; ++j) view_cost_out[item * nv + j] = b.vcost[item * nv + j];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------- k_sad
+// cf_model 1 (HDist_kernels.cu:111-203): per view, sum over mask > 0.5 of
+// |(f - mean f) - (g - mean g)| with the means k_view left in hmean.  The
+// mask is 0 or 1 and a DRR pixel under it is non-zero, so f != 0 marks the
+// pixels under the mask; tiles k_view found without such pixels are skipped.
+// Tile partials in FP32, the view's sum in FP64 by the view's last tile.
+__global__ void __launch_bounds__(256) k_sad(const SceneDev* __restrict__ sc, Bufs b, double* __restrict__ cost,
+                                             double* __restrict__ view_cost_out)
+{
+  __shared__ float red[8];
+  __shared__ double dred[8];
+  __shared__ bool s_last;
+  const int nv = sc->n_views, ftiles = b.C->ftiles;
+  for (int tile = blockIdx.x; tile < ftiles; tile += gridDim.x) {
+    const int k = find_iv(b.foff, b.C->n_iv, tile);
+    const IV& r = b.iv[k];
+    const int t = tile - b.foff[k];
+    const int tx0 = (t % r.ftx) * VT, ty0 = (t / r.ftx) * VT;
+    float a = 0.f;
+    if (b.part[tile].n > 0) {
+      const double2 mu = b.hmean[k];
+      const float mf = (float)mu.x, mg = (float)mu.y;
+      for (int i = threadIdx.x; i < VT * VT; i += blockDim.x) {
+        const int x = tx0 + i % VT, y = ty0 + i / VT;
+        if (x < r.w && y < r.h) {
+          const float2 v = b.fg[r.pix + (long long)y * r.w + x];
+          if (v.x != 0.f) a += fabsf((v.x - mf) - (v.y - mg));
+        }
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float tot = 0.f;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+      b.tsad[tile] = tot;
+      __threadfence();
+      s_last = atomicAdd(&b.ivt[k], 1u) == (unsigned)(r.ftx * r.fty) - 1;
+    }
+    __syncthreads();
+    if (s_last) {
+      __threadfence();
+      const int nt = r.ftx * r.fty, base = b.foff[k];
+      double d = 0.0;
+      for (int i = threadIdx.x; i < nt; i += blockDim.x) d += (double)__ldcg(b.tsad + base + i);
+      for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+      if ((threadIdx.x & 31) == 0) dred[threadIdx.x >> 5] = d;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double vc = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) vc += dred[w];
+        b.vcost[k] = vc;
+        __threadfence();
+        const int item = k / nv;
+        if (atomicAdd(&b.itt[item], 1u) == (unsigned)nv - 1) {
+          __threadfence();
+          finish_item(sc, b, item, cost);
+          if (view_cost_out)
+            for (int j = 0; j < nv; ++j) view_cost_out[item * nv + j] = b.vcost[item * nv + j];
+        }
       }
     }
     __syncthreads();
@@ -883,6 +964,7 @@ struct Swarm {
   double* gx;   // [bone][6]
   double* gc;   // [bone]
   int* iter;
+  int* frozen;  // [bone] the swarm stalled: its particles stay put
   int* bone;    // item -> bone
   double* manip;  // item -> x
 };
@@ -912,6 +994,7 @@ __global__ void k_pso_init(Swarm s, int nb, int np, double lo, double hi, unsign
     int b = i / np;
     for (int d = 0; d < 6; ++d) s.gx[6 * b + d] = 0.0;
     s.gc[b] = 1e300;
+    s.frozen[b] = 0;
   }
   if (i == 0) *s.iter = 0;
 }
@@ -923,6 +1006,11 @@ __global__ void k_pso_update(Swarm s, int nb, int np, double w, double c1, doubl
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nb * np) return;
   int b = i / np;
+  s.bone[i] = b;
+  if (s.frozen[b]) {  // re-scored where it is: the same cost, no best changes
+    for (int d = 0; d < 6; ++d) s.manip[6 * i + d] = s.x[6 * i + d];
+    return;
+  }
   unsigned long long it = (unsigned long long)*s.iter + 1;
   for (int d = 0; d < 6; ++d) {
     unsigned long long c = ((it * (unsigned long long)(nb * np) + i) * 6 + d) * 2;
@@ -933,7 +1021,6 @@ __global__ void k_pso_update(Swarm s, int nb, int np, double w, double c1, doubl
     s.x[6 * i + d] = x + vv;
     s.manip[6 * i + d] = x + vv;
   }
-  s.bone[i] = b;
 }
 
 // pBest / gBest update after an iteration's costs (one block per swarm).
@@ -996,6 +1083,7 @@ struct asc_engine_s {
   // device PSO: swarm state, the captured iteration and a private stream
   double* sw_buf = nullptr;
   int* sw_iter = nullptr;
+  int* sw_frozen = nullptr;
   cudaGraphExec_t pso_exec = nullptr;
   double pso_key[5] = {0, 0, 0, 0, 0};
   cudaStream_t own_stream = nullptr;
@@ -1097,7 +1185,7 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
   if (!views || !bones || !out || n_views < 1 || n_views > MAX_VIEWS || n_bones < 1 || n_bones > MAX_BONES ||
       rw < 1 || rh < 1 || max_items < 1 || (coverage != ASC_SUM_TREE && coverage != ASC_SUM_FULL))
     return ASC_ERR_ARG;
-  if (cf_model != 0) return ASC_ERR_ARG;  // the engine scores NCC; SAD runs through asc_hdist
+  if (cf_model != 0 && cf_model != 1) return ASC_ERR_ARG;
   Gate g(device_gate());
   // set-up work runs on a private stream, so that creating an engine does not
   // wait for other engines' work
@@ -1115,6 +1203,7 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
   S.rw = rw;
   S.rh = rh;
   S.coverage = coverage;
+  S.cf_model = cf_model;
   int hmax = 0;
   for (int v = 0; v < n_views; ++v) {
     int rc = fill_view(S.views[v], views[v]);
@@ -1168,6 +1257,9 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
   if (!err) err = e->alloc(e->b.foff, n_iv + 1);
   if (!err) err = e->alloc(e->b.drr, n_iv * (size_t)rw * rh);
   if (!err) err = e->alloc(e->b.part, n_iv * tiles);
+  if (!err && cf_model) err = e->alloc(e->b.fg, n_iv * (size_t)rw * rh);
+  if (!err && cf_model) err = e->alloc(e->b.hmean, n_iv);
+  if (!err && cf_model) err = e->alloc(e->b.tsad, n_iv * tiles);
   if (!err) err = e->alloc(e->b.vcost, n_iv);
   if (!err) err = e->alloc(e->b.ivt, n_iv);
   if (!err) err = e->alloc(e->b.itt, (size_t)max_items);
@@ -1255,6 +1347,7 @@ static int engine_launch(asc_engine e, int n, const int* bone, const double* man
   k_ray<<<e->sms * ASC_RAY_MINBLOCKS, NRAY, 0, s>>>(e->dev, e->b, g_empty_skip);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[2], s));
   k_view<<<e->sms * e->view_blocks, VNT, e->smem, s>>>(e->dev, e->b, cost, vcost);
+  if (e->host.cf_model) k_sad<<<e->sms * 8, 256, 0, s>>>(e->dev, e->b, cost, vcost);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[3], s));
   if (vcost) k_copy_vcost<<<8, 256, 0, s>>>(e->b.vcost, vcost, n * e->n_views);
   ASC_LAUNCH_CHECK();
@@ -1330,10 +1423,11 @@ ASC_API int asc_engine_debug(asc_engine e, const float** drr, const int** layout
   return ASC_OK;
 }
 
-ASC_API int asc_engine_pso(asc_engine e, int np, int n_iter, double w, double c1, double c2, double lo, double hi,
-                           uint64_t seed, double* best_manip, double* best_cost, long long* evals, void* stream)
+ASC_API int asc_engine_pso_stall(asc_engine e, int np, int n_iter, int max_stall, double w, double c1, double c2,
+                                 double lo, double hi, uint64_t seed, double* best_manip, double* best_cost,
+                                 long long* evals, int* iterations, void* stream)
 {
-  if (!e || np < 1 || n_iter < 1 || !best_manip || !best_cost) return ASC_ERR_ARG;
+  if (!e || np < 1 || n_iter < 1 || max_stall < 0 || !best_manip || !best_cost) return ASC_ERR_ARG;
   const int nb = e->n_bones, n = nb * np;
   if (n > e->max_items) return ASC_ERR_RANGE;
   cudaStream_t s = S(stream);
@@ -1347,6 +1441,7 @@ ASC_API int asc_engine_pso(asc_engine e, int np, int n_iter, double w, double c1
     const size_t cap = (size_t)e->max_items, nbm = (size_t)e->n_bones;
     cudaError_t err = e->alloc(e->sw_buf, cap * 6 * 3 + cap + nbm * 6 + nbm);
     if (!err) err = e->alloc(e->sw_iter, 1);
+    if (!err) err = e->alloc(e->sw_frozen, nbm);
     if (err) return cuda_status(err);
   }
   Swarm sw;
@@ -1357,6 +1452,7 @@ ASC_API int asc_engine_pso(asc_engine e, int np, int n_iter, double w, double c1
   sw.gx = sw.pbc + n;
   sw.gc = sw.gx + nb * 6;
   sw.iter = e->sw_iter;
+  sw.frozen = e->sw_frozen;
   sw.bone = e->d_bone;
   sw.manip = e->d_manip;
   const int tb = 128, gb = (n + tb - 1) / tb;
@@ -1383,12 +1479,53 @@ ASC_API int asc_engine_pso(asc_engine e, int np, int n_iter, double w, double c1
     if (graph) cudaGraphDestroy(graph);
     if (!err) memcpy(e->pso_key, key, sizeof key);
   }
-  for (int it = 0; !err && it < n_iter; ++it) err = cudaGraphLaunch(e->pso_exec, s);
+  long long scored = 0;
+  int it = 0;
+  if (max_stall == 0) {
+    for (; !err && it < n_iter; ++it) err = cudaGraphLaunch(e->pso_exec, s);
+    scored = (long long)n * it;
+  } else {
+    // the stall rule of PSO.cpp:271-285 per swarm, read back after every
+    // iteration: |gBest change| < 1e-4 counts a stall, > 1e-3 resets the
+    // count, max_stall stalls in a row stop that swarm (it is frozen, and
+    // the iterations end when every swarm is)
+    std::vector<double> gc(nb), prev(nb, 1e300);
+    std::vector<int> stall(nb, 0), frozen(nb, 0);
+    int live = nb;
+    for (; !err && it < n_iter && live > 0; ++it) {
+      err = cudaGraphLaunch(e->pso_exec, s);
+      scored += (long long)np * live;
+      if (!err) err = cudaMemcpyAsync(gc.data(), sw.gc, nb * sizeof(double), cudaMemcpyDeviceToHost, s);
+      if (!err) err = cudaStreamSynchronize(s);
+      for (int b = 0; !err && b < nb; ++b) {
+        if (frozen[b]) continue;
+        const double d = std::fabs(gc[b] - prev[b]);
+        if (d < 1e-4)
+          ++stall[b];
+        else if (d > 1e-3)
+          stall[b] = 0;
+        prev[b] = gc[b];
+        if (stall[b] == max_stall) {
+          frozen[b] = 1;
+          --live;
+          err = cudaMemcpyAsync(sw.frozen + b, &frozen[b], sizeof(int), cudaMemcpyHostToDevice, s);
+        }
+      }
+    }
+  }
   if (!err) err = cudaMemcpyAsync(best_manip, sw.gx, nb * 6 * sizeof(double), cudaMemcpyDeviceToHost, s);
   if (!err) err = cudaMemcpyAsync(best_cost, sw.gc, nb * sizeof(double), cudaMemcpyDeviceToHost, s);
   if (!err) err = cudaStreamSynchronize(s);
-  if (evals) *evals = (long long)n * n_iter;
+  if (evals) *evals = scored;
+  if (iterations) *iterations = it;
   return err ? cuda_status(err) : ASC_OK;
+}
+
+ASC_API int asc_engine_pso(asc_engine e, int np, int n_iter, double w, double c1, double c2, double lo, double hi,
+                           uint64_t seed, double* best_manip, double* best_cost, long long* evals, void* stream)
+{
+  return asc_engine_pso_stall(e, np, n_iter, 0, w, c1, c2, lo, hi, seed, best_manip, best_cost, evals, nullptr,
+                              stream);
 }
 
 // ---------------------------------------------------------------- plain path
@@ -1459,7 +1596,7 @@ ASC_API int asc_engine_eval_plain(asc_engine e, int n, const int* bone, const do
         unsigned w = fw > 0 ? (unsigned)fw : 0u, h = fh > 0 ? (unsigned)fh : 0u;
         if (w > (unsigned)S_.rw || h > (unsigned)S_.rh) return ASC_ERR_RANGE;
         if (w == 0 || h == 0) {
-          vc = 1.0 - 1e5;
+          vc = S_.cf_model ? 0.0 : 1.0 - 1e5;
         } else {
           float vpf[4] = {(float)vp[0], (float)vp[1], (float)vp[2], (float)vp[3]};
           int rc = raycast_launch(B.vol, g_empty_skip ? B.occ[v] : nullptr, m, vpf, BD.step[v], BD.intensity[v],
@@ -1481,15 +1618,17 @@ ASC_API int asc_engine_eval_plain(asc_engine e, int n, const int* bone, const do
           if (!rc) rc = asc_multiply(bgm, mask, mask, w, h, s);
           if (!rc) rc = asc_multiply(r, mask, r, w, h, s);
           if (!rc) rc = asc_multiply(d, mask, d, w, h, s);
-          double ncc = 0;
-          if (!rc) rc = asc_ncc(d, r, mask, w * h, S_.coverage, e->p_res, s);
+          double res = 0;
+          if (!rc)
+            rc = S_.cf_model ? asc_hdist(d, r, mask, w * h, S_.coverage, e->p_res, s)
+                             : asc_ncc(d, r, mask, w * h, S_.coverage, e->p_res, s);
           if (!rc) {
-            cudaError_t err = cudaMemcpyAsync(&ncc, e->p_res, sizeof(double), cudaMemcpyDeviceToHost, s);
+            cudaError_t err = cudaMemcpyAsync(&res, e->p_res, sizeof(double), cudaMemcpyDeviceToHost, s);
             if (!err) err = cudaStreamSynchronize(s);
             if (err) rc = cuda_status(err);
           }
           if (rc) return rc;
-          vc = 1.0 - ncc;
+          vc = S_.cf_model ? res : 1.0 - res;  // Tracker.cpp:762-770
         }
       }
       if (view_cost) view_cost[it * nv + v] = vc;
@@ -1565,8 +1704,8 @@ ASC_API int asc_engine_optimize_frame(asc_engine e, const asc_opt_params* p, dou
     // final composition starts from the unrounded one (Tracker.cpp:445-491)
     std::vector<double> best(6 * nb), bc(nb);
     long long ev = 0;
-    rc = asc_engine_pso(e, p->n_particles, p->n_iter, p->w, p->c1, p->c2, p->lo, p->hi, p->seed, best.data(), bc.data(),
-                        &ev, (void*)s);
+    rc = asc_engine_pso_stall(e, p->n_particles, p->n_iter, p->max_stall, p->w, p->c1, p->c2, p->lo, p->hi, p->seed,
+                              best.data(), bc.data(), &ev, nullptr, (void*)s);
     if (rc) return rc;
     ctx.evals += ev;
     for (int b = 0; b < nb; ++b) {

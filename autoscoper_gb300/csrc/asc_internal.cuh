@@ -275,24 +275,45 @@ inline void frame_linear_extrap(const double* a, const double* b, double* out)
   out[11] += trans[2];
 }
 
+// A float quaternion (Quat<float>: w, x, y, z).
+struct QuatF {
+  float w, x, y, z;
+};
+
+// Quat<float>(yaw, pitch, roll) (Quaternion.hpp:80-94), degrees, float math.
+inline QuatF quat_from_ypr(float yaw, float pitch, float roll)
+{
+  const float pi = (float)3.14159265358979323846;
+  const float cr = cosf(roll * pi / 360.0f), sr = sinf(roll * pi / 360.0f);
+  const float cp = cosf(pitch * pi / 360.0f), sp = sinf(pitch * pi / 360.0f);
+  const float cy = cosf(yaw * pi / 360.0f), sy = sinf(yaw * pi / 360.0f);
+  return {cr * cp * cy + sr * sp * sy, sr * cp * cy - cr * sp * sy, cr * sp * cy + sr * cp * sy,
+          cr * cp * sy - sr * sp * cy};
+}
+
+// Quat<float>::toEuler (Quaternion.hpp:220-243) read as (yaw, pitch, roll) =
+// (e.z, e.y, e.x), degrees.
+inline void quat_to_ypr(const QuatF& q, double* ypr)
+{
+  const float pi = (float)3.14159265358979323846;
+  const float w = q.w, x = q.x, y = q.y, z = q.z;
+  const float rx = atan2f(2.0f * (w * x + y * z), 1.0f - 2.0f * (x * x + y * y));
+  const float ry = 2.0f * atan2f(sqrtf(1.0f + 2.0f * (w * y - x * z)), sqrtf(1.0f - 2.0f * (w * y - x * z))) - pi / 2.0f;
+  const float rz = atan2f(2.0f * (w * z + x * y), 1.0f - 2.0f * (y * y + z * z));
+  ypr[0] = rz * (180.0f / pi);
+  ypr[1] = ry * (180.0f / pi);
+  ypr[2] = rx * (180.0f / pi);
+}
+
 // The pose a trial's key curves hold after Tracker::optimize stores v and
 // reads it back (Tracker.cpp:422-438): x, y, z as float; the rotation as a
 // float quaternion from (yaw, pitch, roll) (Quaternion.hpp:80-94) read back
 // as Euler angles (Quaternion.hpp:220-243), in float math as there.
 inline void keycurve_store(const double* v, double* out)
 {
-  const float pi = (float)3.14159265358979323846;
-  const float yaw = (float)v[3], pitch = (float)v[4], roll = (float)v[5];
-  const float cr = cosf(roll * pi / 360.0f), sr = sinf(roll * pi / 360.0f);
-  const float cp = cosf(pitch * pi / 360.0f), sp = sinf(pitch * pi / 360.0f);
-  const float cy = cosf(yaw * pi / 360.0f), sy = sinf(yaw * pi / 360.0f);
-  const float w = cr * cp * cy + sr * sp * sy, x = sr * cp * cy - cr * sp * sy;
-  const float y = cr * sp * cy + sr * cp * sy, z = cr * cp * sy - sr * sp * cy;
-  const float rx = atan2f(2.0f * (w * x + y * z), 1.0f - 2.0f * (x * x + y * y));
-  const float ry = 2.0f * atan2f(sqrtf(1.0f + 2.0f * (w * y - x * z)), sqrtf(1.0f - 2.0f * (w * y - x * z))) - pi / 2.0f;
-  const float rz = atan2f(2.0f * (w * z + x * y), 1.0f - 2.0f * (y * y + z * z));
-  const double o[6] = {(float)v[0], (float)v[1], (float)v[2], rz * (180.0f / pi), ry * (180.0f / pi),
-                       rx * (180.0f / pi)};
+  const QuatF q = quat_from_ypr((float)v[3], (float)v[4], (float)v[5]);
+  double o[6] = {(float)v[0], (float)v[1], (float)v[2], 0, 0, 0};
+  quat_to_ypr(q, o + 3);
   for (int i = 0; i < 6; ++i) out[i] = o[i];
 }
 

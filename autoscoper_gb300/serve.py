@@ -73,6 +73,8 @@ def engine_bytes(scene: S.Scene, max_items: int) -> int:
     n_iv = max_items * nv
     tiles = ((rw + 31) // 32) * ((rh + 31) // 32)
     b = n_iv * rw * rh * 4 + n_iv * tiles * 72 + 7 * rw * rh * 4 + n_iv * 160 + max_items * 200
+    if scene.cf_model:  # SAD: f and g per crop pixel, tile sums, view means
+        b += n_iv * rw * rh * 8 + n_iv * tiles * 4 + n_iv * 16
     b += sum(v.radiograph.nbytes for v in scene.views)
     return b
 

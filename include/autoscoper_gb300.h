@@ -227,6 +227,8 @@ typedef struct {
   float step[4], intensity[4], cutoff[4];  /* RayCaster settings per view */
 } asc_bone_desc;
 
+/* cf_model (Tracker::optimize's cf_model, Tracker.cpp:762-770): 0 scores a
+ * view by 1 - NCC, 1 by the SAD of gpu::hdist (HDist_kernels.cu:111-203). */
 int asc_engine_create(int n_views, const asc_view_desc *views, int n_bones, const asc_bone_desc *bones,
                       int render_width, int render_height, int max_items, int coverage, int cf_model,
                       asc_engine *out);
@@ -273,6 +275,14 @@ int asc_engine_counters(asc_engine e, unsigned long long out[4]);
  * bone) receive gBest.  evals_out (optional) the number of poses scored. */
 int asc_engine_pso(asc_engine e, int n_particles, int n_iter, double w, double c1, double c2, double lo, double hi,
                    uint64_t seed, double *best_manip, double *best_cost, long long *evals_out, void *stream);
+/* asc_engine_pso with the stall rule of pso() (PSO.cpp:271-285) per bone:
+ * after each iteration a gBest change below 1e-4 counts a stall, one above
+ * 1e-3 resets the count; max_stall stalls in a row stop that bone's swarm,
+ * and the iterations end when every swarm has stopped or after n_iter
+ * (max_stall 0: never stalls).  iterations_out (optional): iterations run. */
+int asc_engine_pso_stall(asc_engine e, int n_particles, int n_iter, int max_stall, double w, double c1, double c2,
+                         double lo, double hi, uint64_t seed, double *best_manip, double *best_cost,
+                         long long *evals_out, int *iterations_out, void *stream);
 
 /* Many Nelder-Mead simplices in lock-step (AMOEBA, DownhillSimplex.cpp:39-172):
  * each iteration evaluates, per simplex, the reflection and speculatively the
@@ -299,6 +309,7 @@ typedef struct {
   uint64_t seed;
   double offsets[6];   /* initial simplex offsets (Trial::offsets, default 0.1) */
   double ftol;         /* 1e-3 in the reference */
+  int max_stall;       /* PSO stall limit (asc_engine_pso_stall); 0: n_iter iterations */
 } asc_opt_params;
 int asc_engine_optimize_frame(asc_engine e, const asc_opt_params *params, double *pose_out, double *cost_out,
                               long long *evals_out, void *stream);
@@ -322,6 +333,29 @@ int asc_engine_image_data(asc_engine e, int view, int bone, const double pose[6]
  * KeyCurve<Quatf>): x, y, z rounded to float, the rotation through a float
  * quaternion.  Host arithmetic only. */
 int asc_keycurve_store(const double pose[6], double out[6]);
+
+/* A volume's pose curves over frames (Trial::getXCurve/.../getQuatCurve):
+ * x, y, z as KeyCurve<float> (cubic segments between keys with SMOOTH
+ * tangents, KeyCurve.hpp:231-446) and the rotation as KeyCurve<Quatf>
+ * (slerp between keys, Quaternion.hpp:380-403).  insert stores a pose at a
+ * frame in the curves named by `mask` as AutoscoperMainWindow::setPose does
+ * (x, y, z as float; Quatf(yaw, pitch, roll)); erase removes their keys at a
+ * frame; eval reads the pose at a frame as getPose does (the curves'
+ * values, the rotation's toEuler as yaw, pitch, roll); keys reports which
+ * curves hold a key at a frame.  Host arithmetic only. */
+typedef struct asc_pose_curve_s *asc_pose_curve;
+#define ASC_CURVE_X 1
+#define ASC_CURVE_Y 2
+#define ASC_CURVE_Z 4
+#define ASC_CURVE_ROT 8
+#define ASC_CURVE_ALL 15
+int asc_pose_curve_create(asc_pose_curve *out);
+int asc_pose_curve_destroy(asc_pose_curve c);
+int asc_pose_curve_clear(asc_pose_curve c);
+int asc_pose_curve_insert(asc_pose_curve c, int frame, const double xyzypr[6], int mask);
+int asc_pose_curve_erase(asc_pose_curve c, int frame, int mask);
+int asc_pose_curve_keys(asc_pose_curve c, int frame, int *mask);
+int asc_pose_curve_eval(asc_pose_curve c, int frame, double xyzypr[6]);
 
 /* A sequence of Tracker::optimize calls (Tracker.cpp:337-580), frames in
  * order (dframe +1) or in reverse (dframe -1).  Per frame: the views take

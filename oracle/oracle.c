@@ -23,6 +23,7 @@
  *    linear filtering and clamp-to-edge addressing
  *    (libautoscoper/src/gpu/cuda/cutil/cutil_create_tex_obj.h:6-28).
  */
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -161,27 +162,127 @@ ORC_EXPORT void orc_frame_linear_extrap(const double a[12], const double b[12], 
  * it back (Tracker.cpp:422-438): x, y, z as float; the rotation as a float
  * quaternion from (yaw, pitch, roll) (Quaternion.hpp:80-94), read back as
  * Euler angles (Quaternion.hpp:220-243).  Float math throughout, as there. */
-ORC_EXPORT void orc_keycurve_store(const double in[6], double out[6])
+/* Quat<float>(yaw, pitch, roll), Quaternion.hpp:80-94: q = (w, x, y, z). */
+ORC_EXPORT void orc_quat_from_ypr(float yaw, float pitch, float roll, float q[4])
 {
   const float pi = (float)M_PI;
-  const float yaw = (float)in[3], pitch = (float)in[4], roll = (float)in[5];
   const float cr = cosf(roll * pi / 360.0f), sr = sinf(roll * pi / 360.0f);
   const float cp = cosf(pitch * pi / 360.0f), sp = sinf(pitch * pi / 360.0f);
   const float cy = cosf(yaw * pi / 360.0f), sy = sinf(yaw * pi / 360.0f);
-  const float w = cr * cp * cy + sr * sp * sy;
-  const float x = sr * cp * cy - cr * sp * sy;
-  const float y = cr * sp * cy + sr * cp * sy;
-  const float z = cr * cp * sy - sr * sp * cy;
+  q[0] = cr * cp * cy + sr * sp * sy;
+  q[1] = sr * cp * cy - cr * sp * sy;
+  q[2] = cr * sp * cy + sr * cp * sy;
+  q[3] = cr * cp * sy - sr * sp * cy;
+}
+
+/* Quat<float>::toEuler, Quaternion.hpp:220-243, read as (yaw, pitch, roll)
+   = (e.z, e.y, e.x) in degrees. */
+ORC_EXPORT void orc_quat_to_ypr(const float q[4], double ypr[3])
+{
+  const float pi = (float)M_PI;
+  const float w = q[0], x = q[1], y = q[2], z = q[3];
   const float r_x = atan2f(2.0f * (w * x + y * z), 1.0f - 2.0f * (x * x + y * y));
   const float sp2 = sqrtf(1.0f + 2.0f * (w * y - x * z)), cp2 = sqrtf(1.0f - 2.0f * (w * y - x * z));
   const float r_y = 2.0f * atan2f(sp2, cp2) - pi / 2.0f;
   const float r_z = atan2f(2.0f * (w * z + x * y), 1.0f - 2.0f * (y * y + z * z));
+  ypr[0] = r_z * (180.0f / pi);
+  ypr[1] = r_y * (180.0f / pi);
+  ypr[2] = r_x * (180.0f / pi);
+}
+
+ORC_EXPORT void orc_keycurve_store(const double in[6], double out[6])
+{
+  float q[4];
+  orc_quat_from_ypr((float)in[3], (float)in[4], (float)in[5], q);
   out[0] = (float)in[0];
   out[1] = (float)in[1];
   out[2] = (float)in[2];
-  out[3] = r_z * (180.0f / pi);
-  out[4] = r_y * (180.0f / pi);
-  out[5] = r_x * (180.0f / pi);
+  orc_quat_to_ypr(q, out + 3);
+}
+
+/* KeyCurve<float>::operator() (KeyCurve.hpp:334-359) over keys (times
+   ascending, float values), every key SMOOTH: the tangent of key i is
+   (v[i+1] - v[i-1]) / (t[i+1] - t[i-1]) with the neighbours clamped to the
+   ends (update_curve, KeyCurve.hpp:403-426), and the segment from key i is
+   the cubic a + b s + c s^2 + d s^3 with D1 = tan_i (t[i+1] - t[i]),
+   D2 = tan_{i+1} (t[i+1] - t[i]) (KeyCurve.hpp:428-441).  Here every
+   tangent and segment is computed afresh from the final keys. */
+static float curve_tangent(int n, const int *t, const float *v, int i)
+{
+  const int p = i > 0 ? i - 1 : i, q = i < n - 1 ? i + 1 : i;
+  return (v[q] - v[p]) / (float)(t[q] - t[p]);
+}
+
+ORC_EXPORT float orc_curve_eval(int n, const int *t, const float *v, int frame)
+{
+  if (n == 0) return 0.0f;
+  int j = 0; /* first key after frame */
+  while (j < n && t[j] <= frame) ++j;
+  if (j == 0) return v[0];
+  if (j == n) return v[n - 1];
+  const int i = j - 1;
+  const float ti = (float)t[i], dt = (float)t[j] - ti;
+  const float D1 = curve_tangent(n, t, v, i) * dt, D2 = curve_tangent(n, t, v, j) * dt;
+  const float a = v[i], b = D1;
+  const float c = 3.0f * (v[j] - v[i]) - 2.0f * D1 - D2;
+  const float d = 2.0f * (v[i] - v[j]) + D1 + D2;
+  const float s = ((float)frame - ti) / (float)(t[j] - t[i]);
+  return a + s * b + s * s * c + s * s * s * d;
+}
+
+static float q4_dot(const float *p, const float *q) { return p[0] * q[0] + p[1] * q[1] + p[2] * q[2] + p[3] * q[3]; }
+static void q4_unit(const float *q, float *o)
+{
+  const float l = sqrtf(q4_dot(q, q));
+  for (int k = 0; k < 4; ++k) o[k] = q[k] / l;
+}
+
+/* KeyCurve<Quatf>::operator(): slerp (Quaternion.hpp:380-396) between the
+   keys around frame, nlerp (:400-403) for nearly equal ones; q: 4 floats
+   (w, x, y, z) per key. */
+ORC_EXPORT void orc_quat_curve_eval(int n, const int *t, const float *q, int frame, float out[4])
+{
+  if (n == 0) {
+    out[0] = 1.0f;
+    out[1] = out[2] = out[3] = 0.0f;
+    return;
+  }
+  int j = 0;
+  while (j < n && t[j] <= frame) ++j;
+  const float *src = j == 0 ? q : q + 4 * (j - 1);
+  if (j == 0 || j == n) {
+    for (int k = 0; k < 4; ++k) out[k] = src[k];
+    return;
+  }
+  const float *p0 = q + 4 * (j - 1), *p1 = q + 4 * j;
+  const float s = ((float)frame - (float)t[j - 1]) / (float)(t[j] - t[j - 1]);
+  float r[4], u0[4], u1[4];
+  if (s < FLT_EPSILON) {
+    for (int k = 0; k < 4; ++k) out[k] = p0[k];
+    return;
+  }
+  if (s > 1.0f - FLT_EPSILON) {
+    for (int k = 0; k < 4; ++k) out[k] = p1[k];
+    return;
+  }
+  q4_unit(p0, u0);
+  q4_unit(p1, u1);
+  const float cr = q4_dot(u0, u1);
+  float rad = acosf(cr);
+  if (rad < FLT_EPSILON) {
+    if (q4_dot(p0, p1) > 0.0f)
+      for (int k = 0; k < 4; ++k) r[k] = p0[k] + s * (p1[k] - p0[k]);
+    else
+      for (int k = 0; k < 4; ++k) r[k] = p0[k] - s * (p1[k] + p0[k]);
+  } else if (cr > 0.0f) {
+    const float a = sinf(rad * (1.0f - s)), b = sinf(rad * s);
+    for (int k = 0; k < 4; ++k) r[k] = a * p0[k] + b * p1[k];
+  } else {
+    rad = (float)(M_PI - (double)rad);
+    const float a = sinf(rad * (1.0f - s)), b = sinf(rad * s);
+    for (int k = 0; k < 4; ++k) r[k] = a * p0[k] - b * p1[k];
+  }
+  q4_unit(r, out);
 }
 
 /* ------------------------------------------------------------------ */

@@ -78,6 +78,11 @@ def lib():
         for n in ("orc_frame_mul", "orc_frame_linear_extrap"):
             getattr(L, n).argtypes = [_d, _d, _d]
         L.orc_camera_viewport.argtypes = [C.c_double] * 6 + [_d]
+        L.orc_quat_from_ypr.argtypes = [C.c_float, C.c_float, C.c_float, _f]
+        L.orc_quat_to_ypr.argtypes = [_f, _d]
+        L.orc_curve_eval.argtypes = [C.c_int, _i, _f, C.c_int]
+        L.orc_curve_eval.restype = C.c_float
+        L.orc_quat_curve_eval.argtypes = [C.c_int, _i, _f, C.c_int, _f]
         L.orc_camera_image_plane.argtypes = [_d] + [C.c_double] * 5 + [_d]
     return _LIB
 
@@ -141,6 +146,48 @@ def keycurve_store(v):
     out = np.zeros(6)
     lib().orc_keycurve_store(_dp(_arr(v)), _dp(out))
     return out
+
+
+class PoseCurves:
+    """A volume's pose curves (x, y, z KeyCurve<float>, rotation
+    KeyCurve<Quatf>): the keys of each curve as frame -> stored value, and
+    the value at a frame computed afresh from the final keys
+    (orc_curve_eval, orc_quat_curve_eval)."""
+
+    def __init__(self):
+        self.keys = [{}, {}, {}, {}]   # x, y, z: float32; rotation: float32 (w, x, y, z)
+
+    def clear(self):
+        self.keys = [{}, {}, {}, {}]
+
+    def insert(self, frame, pose, mask=15):
+        for c in range(3):
+            if mask >> c & 1:
+                self.keys[c][frame] = np.float32(pose[c])
+        if mask & 8:
+            q = np.zeros(4, np.float32)
+            lib().orc_quat_from_ypr(*(float(np.float32(pose[k])) for k in (3, 4, 5)), q.ctypes.data_as(_f))
+            self.keys[3][frame] = q
+
+    def erase(self, frame, mask=15):
+        for c in range(4):
+            if mask >> c & 1:
+                self.keys[c].pop(frame, None)
+
+    def eval(self, frame):
+        out = np.zeros(6)
+        for c in range(3):
+            t = np.array(sorted(self.keys[c]), np.int32)
+            v = np.array([self.keys[c][f] for f in t], np.float32)
+            out[c] = lib().orc_curve_eval(len(t), t.ctypes.data_as(_i), v.ctypes.data_as(_f), int(frame))
+        t = np.array(sorted(self.keys[3]), np.int32)
+        q = np.array([self.keys[3][f] for f in t], np.float32).reshape(-1)
+        r = np.zeros(4, np.float32)
+        lib().orc_quat_curve_eval(len(t), t.ctypes.data_as(_i), q.ctypes.data_as(_f), int(frame), r.ctypes.data_as(_f))
+        ypr = np.zeros(3)
+        lib().orc_quat_to_ypr(r.ctypes.data_as(_f), _dp(ypr))
+        out[3:] = ypr
+        return out
 
 
 def camera_viewport(cx, cy, fx, fy, W, H):

@@ -77,6 +77,7 @@ def lib():
             getattr(L, n).argtypes = [_d, _d]
         for n in ("ref_frame_mul", "ref_frame_linear_extrap"):
             getattr(L, n).argtypes = [_d, _d, _d]
+        L.ref_pose_curve_run.argtypes = [C.c_int, _i, _i, _i, _d, C.c_int, _i, _d]
         L.ref_pso.argtypes = [COST_FN, C.c_void_p, C.c_float, C.c_float, C.c_uint, C.c_uint, C.c_uint, _f, _f]
         L.ref_amoeba.argtypes = [COST_FN, C.c_void_p, _d, _d, C.c_int, C.c_double]
         L.ref_amoeba.restype = C.c_int
@@ -104,6 +105,21 @@ def f64(a):
 def frame_op(name, *args, n_out=12):
     out = np.zeros(n_out)
     getattr(lib(), name)(*[_dp(f64(a)) for a in args], _dp(out))
+    return out
+
+
+def pose_curve_run(ops, eval_frames):
+    """The reference's KeyCurve<float> x, y, z and KeyCurve<Quatf> driven by
+    ops [(kind, frame, mask, pose)], read at eval_frames: (len, 6) poses."""
+    n = len(ops)
+    kinds = np.array([o[0] for o in ops], np.int32)
+    frames = np.array([o[1] for o in ops], np.int32)
+    masks = np.array([o[2] for o in ops], np.int32)
+    poses = f64(np.array([o[3] for o in ops]).reshape(n, 6))
+    ev = np.array(eval_frames, np.int32)
+    out = np.zeros((len(ev), 6))
+    lib().ref_pose_curve_run(n, kinds.ctypes.data_as(_i), frames.ctypes.data_as(_i), masks.ctypes.data_as(_i),
+                             _dp(poses), len(ev), ev.ctypes.data_as(_i), _dp(out))
     return out
 
 

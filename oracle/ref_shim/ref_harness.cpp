@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "CoordFrame.hpp"
+#include "KeyCurve.hpp"
 #include "Quaternion.hpp"
 #include "DownhillSimplex.hpp"
 #include "PSO.hpp"
@@ -61,6 +62,45 @@ REF_EXPORT void ref_keycurve_store(const double in[6], double out[6])
   const Vec3f e = q.toEuler();
   const double o[6] = {x, y, z, e.z, e.y, e.x};
   for (int i = 0; i < 6; ++i) out[i] = o[i];
+}
+
+// ---- KeyCurve ----
+// A volume's pose curves (x, y, z KeyCurve<float>, rotation KeyCurve<Quatf>)
+// driven by a list of operations: kind 0 inserts poses[6 i] at frames[i] into
+// the curves of masks[i] (bit 0 x, 1 y, 2 z, 3 rotation) as setPose does,
+// kind 1 erases their keys there, kind 2 clears all; then each of n_eval
+// frames is read back as getPose does (the rotation's toEuler as z, y, x).
+REF_EXPORT void ref_pose_curve_run(int n_ops, const int* kinds, const int* frames, const int* masks,
+                                   const double* poses, int n_eval, const int* eval_frames, double* out)
+{
+  KeyCurve<float> cx(IKeyCurve::X_CURVE), cy(IKeyCurve::Y_CURVE), cz(IKeyCurve::Z_CURVE);
+  KeyCurve<Quatf> cq(IKeyCurve::QUAT_CURVE);
+  for (int i = 0; i < n_ops; ++i) {
+    const int f = frames[i], m = masks[i];
+    const double* p = poses + 6 * i;
+    if (kinds[i] == 0) {
+      if (m & 1) cx.insert(f, p[0]);
+      if (m & 2) cy.insert(f, p[1]);
+      if (m & 4) cz.insert(f, p[2]);
+      if (m & 8) cq.insert(f, Quatf(p[3], p[4], p[5]));
+    } else if (kinds[i] == 1) {
+      if ((m & 1) && cx.find(f) != cx.end()) cx.erase(cx.find(f));
+      if ((m & 2) && cy.find(f) != cy.end()) cy.erase(cy.find(f));
+      if ((m & 4) && cz.find(f) != cz.end()) cz.erase(cz.find(f));
+      if ((m & 8) && cq.find(f) != cq.end()) cq.erase(cq.find(f));
+    } else {
+      cx.clear();
+      cy.clear();
+      cz.clear();
+      cq.clear();
+    }
+  }
+  for (int i = 0; i < n_eval; ++i) {
+    const unsigned int f = (unsigned int)eval_frames[i];
+    const Vec3f e = cq(f).toEuler();
+    const double o[6] = {cx(f), cy(f), cz(f), e.z, e.y, e.x};
+    for (int j = 0; j < 6; ++j) out[6 * i + j] = o[j];
+  }
 }
 
 REF_EXPORT void ref_frame_row_matrix(const double a[12], double m[16]) { to_cf(a).to_matrix_row_order(m); }

@@ -114,3 +114,45 @@ def test_keycurve_store_matches_oracle(lib):
         _lib.call("asc_keycurve_store", v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                   out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
         assert np.array_equal(out, O.keycurve_store(v)), (v, out, O.keycurve_store(v))
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_pose_curves_match_oracle(lib, seed):
+    """asc_pose_curve (KeyCurve<float> x, y, z and KeyCurve<Quatf>, updated
+    key by key as the reference does) against the oracle, which recomputes
+    every tangent and segment from the final keys: bit-identical poses at
+    every frame after every operation (NaN where both give NaN)."""
+    import curve_cases
+    from autoscoper_gb300 import api
+    c, o = api.PoseCurve(), O.PoseCurves()
+    for kind, f, mask, p in curve_cases.ops(seed):
+        if kind == 0:
+            c.insert(f, p, mask)
+            o.insert(f, p, mask)
+        elif kind == 1:
+            c.erase(f, mask)
+            o.erase(f, mask)
+        else:
+            c.clear()
+            o.clear()
+        for g in (f, f + 1, curve_cases.N_FRAMES - 1):
+            km = sum(1 << k for k in range(4) if g in o.keys[k])
+            assert c.keys(g) == km
+        for g in curve_cases.eval_frames():
+            a, b = c.eval(g), o.eval(g)
+            assert np.array_equal(a, b, equal_nan=True), (seed, g, a, b)
+
+
+def test_pose_curve_reads(lib):
+    """Empty curves read the zero pose; one key is held at every frame; a
+    stored key reads back as the key curves store it."""
+    from autoscoper_gb300 import api
+    c = api.PoseCurve()
+    assert np.array_equal(c.eval(3), np.zeros(6))
+    p = np.array([1.25, -3.5, 7.0, 20.0, -10.0, 5.0])
+    c.insert(4, p)
+    for f in (0, 4, 9):
+        assert np.array_equal(c.eval(f), O.keycurve_store(p))
+    assert c.keys(4) == 15 and c.keys(5) == 0
+    c.erase(4, 8)
+    assert c.keys(4) == 7 and np.array_equal(c.eval(4)[3:], np.zeros(3))

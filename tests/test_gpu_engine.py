@@ -66,6 +66,38 @@ def test_engine_and_plain_match_oracle(scene, coverage):
                 assert abs(n_got - n_ref) <= TOL_REL * max(abs(n_ref), 1e-3) + TOL_ABS, (n_got, n_ref)
 
 
+@pytest.mark.parametrize("coverage", [L.ASC_SUM_TREE, L.ASC_SUM_FULL])
+def test_engine_sad_cost_model_matches_oracle(scene, coverage):
+    """cf_model 1 (Tracker.cpp:762-766): each view scores the SAD of
+    gpu::hdist, batched (k_view then k_sad) and plain, against the oracle;
+    per view within 1e-5 relative of the SAD."""
+    import copy
+    sc = copy.copy(scene[0])
+    sc.cf_model = 1
+    tr = O.Tracker(sc, tree=coverage == L.ASC_SUM_TREE)
+    eng = api.Engine(sc, max_items=32, coverage=coverage)
+    rng = np.random.default_rng(21)
+    bones, man = _cands(rng, 12, len(sc.volumes))
+    man[-1] = [0, 0, 5000.0, 0, 0, 0]  # out of view: 9999 per view
+    cost, vcost = eng.eval(bones, man)
+    pcost, pvcost = eng.eval(bones, man, plain=True)
+    for k in range(len(bones)):
+        refv = tr.track_frame(int(bones[k]), tr.compose(int(bones[k]), man[k]))
+        ref = tr.minimization_func(int(bones[k]), man[k])
+        assert ref == pytest.approx(sum(refv))
+        for got in (cost[k], pcost[k]):
+            assert abs(got - ref) <= TOL_REL * abs(ref) + TOL_ABS, (got, ref)
+        for v in range(2):
+            assert refv[v] > 0
+            for got in (vcost[k, v], pvcost[k, v]):
+                assert abs(got - refv[v]) <= TOL_REL * refv[v] + TOL_ABS, (k, v, got, refv[v])
+    assert np.all(vcost[-1] == 9999.0)
+    # the batch is order independent in this mode too
+    perm = rng.permutation(len(bones))
+    c2, _ = eng.eval(bones[perm], man[perm])
+    assert np.array_equal(cost[perm], c2)
+
+
 def test_engine_out_of_view_penalty(scene):
     sc, tr = scene
     eng = api.Engine(sc, max_items=4)
@@ -139,3 +171,11 @@ def test_pso_converges():
         c0 = tr.minimization_func(b, np.zeros(6))
         assert cost[b] < c0
         _check(cost[b], tr.minimization_func(b, best[b]))
+    # the stall rule stops each swarm once its gBest stops moving
+    best2, cost2, ev2 = eng.pso(n_particles=48, n_iter=400, lo=-3, hi=3, seed=3, max_stall=3)
+    its = eng.last_pso_iterations
+    assert 3 <= its < 400
+    assert 48 * its <= ev2 <= 2 * 48 * its
+    for b in range(2):
+        assert cost2[b] < tr.minimization_func(b, np.zeros(6))
+        _check(cost2[b], tr.minimization_func(b, best2[b]))

@@ -196,3 +196,26 @@ def test_amoeba_matches_reference(ref_lib):
     Pb, Yb = P.copy(), Y.copy()
     itb = O.amoeba(_quadratic, Pb, Yb, 1e-3)
     assert ita == itb and np.array_equal(Pa, Pb) and np.array_equal(Ya, Yb)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_pose_curves_bit_exact(ref_lib, seed):
+    """The oracle's pose curves (every tangent and segment recomputed from the
+    final keys) against the reference's KeyCurve.hpp updated key by key, after
+    every prefix of a seeded insert/erase/clear sequence: bit-identical
+    (NaN where the reference's slerp gives NaN)."""
+    import curve_cases
+    ops = curve_cases.ops(seed)
+    frames = curve_cases.eval_frames()
+    o = O.PoseCurves()
+    for i, (kind, f, mask, p) in enumerate(ops):
+        if kind == 0:
+            o.insert(f, p, mask)
+        elif kind == 1:
+            o.erase(f, mask)
+        else:
+            o.clear()
+        if i % 5 == 4 or i == len(ops) - 1:
+            ref = ref_lib.pose_curve_run(ops[:i + 1], frames)
+            got = np.array([o.eval(g) for g in frames])
+            assert np.array_equal(got, ref, equal_nan=True), (seed, i)
