@@ -100,6 +100,7 @@ SIGNATURES = {
     "asc_engine_destroy": (i32, [vp]),
     "asc_engine_set_base_pose": (i32, [vp, i32, P(f64)]),
     "asc_engine_set_radiograph": (i32, [vp, i32, vp]),
+    "asc_engine_set_visible": (i32, [vp, i32, i32]),
     "asc_engine_eval": (i32, [vp, i32, vp, vp, vp, vp, vp]),
     "asc_engine_eval_host": (i32, [vp, i32, P(i32), P(f64), P(f64), P(f64), vp]),
     "asc_engine_eval_plain": (i32, [vp, i32, P(i32), P(f64), P(f64), P(f64), vp]),
@@ -115,7 +116,11 @@ SIGNATURES = {
     "asc_amoeba": (i32, [COST_FN, vp, P(f64), P(f64), i32, f64, P(i32)]),
     "asc_amoeba_batch": (i32, [BATCH_COST_FN, vp, i32, P(f64), P(f64), i32, f64, P(i32)]),
     "asc_engine_optimize_frame": (i32, [vp, P(OptParams), P(f64), P(f64), P(C.c_longlong), vp]),
+    "asc_engine_optimize_frame_ex": (i32, [vp, P(OptParams), P(f64), P(f64), P(f64), P(C.c_longlong), vp]),
     "asc_keycurve_store": (i32, [P(f64), P(f64)]),
+    "asc_engine_optimize_curves": (i32, [vp, P(vp), i32, i32, P(TrackParams), P(f64), P(C.c_longlong), vp]),
+    "asc_pose_to_matrix": (i32, [P(f64), P(f64)]),
+    "asc_pose_from_matrix": (i32, [P(f64), P(f64)]),
     "asc_pose_curve_create": (i32, [P(vp)]),
     "asc_pose_curve_destroy": (i32, [vp]),
     "asc_pose_curve_clear": (i32, [vp]),

@@ -263,9 +263,15 @@ class Engine:
         self.n_views = nv
         self.max_items = max_items
 
-    def set_base_pose(self, bone, xyzypr):
-        _, p = _d(np.asarray(xyzypr, np.float32).astype(np.float64))
+    def set_base_pose(self, bone, xyzypr, exact=False):
+        """The bone's pose; rounded to float as the key curves hold poses
+        unless `exact` (a pose given in double, as getNCC's)."""
+        v = np.asarray(xyzypr, np.float64) if exact else np.asarray(xyzypr, np.float32).astype(np.float64)
+        _, p = _d(v)
         L.call("asc_engine_set_base_pose", self.handle, bone, p)
+
+    def set_visible(self, bone, visible):
+        L.call("asc_engine_set_visible", self.handle, bone, int(bool(visible)))
 
     def set_radiograph(self, view, img: DeviceImage):
         L.call("asc_engine_set_radiograph", self.handle, view, img.handle)
@@ -309,10 +315,13 @@ class Engine:
         p = L.OptParams(method, n_particles, n_iter, w, c1, c2, lo, hi, seed, (C.c_double * 6)(*offsets), ftol,
                         max_stall)
         poses = np.zeros((nb, 6))
+        raw = np.zeros((nb, 6))
         cost = np.zeros(nb)
         ev = C.c_longlong()
-        L.call("asc_engine_optimize_frame", self.handle, C.byref(p), poses.ctypes.data_as(C.POINTER(C.c_double)),
-               cost.ctypes.data_as(C.POINTER(C.c_double)), C.byref(ev), None)
+        L.call("asc_engine_optimize_frame_ex", self.handle, C.byref(p), poses.ctypes.data_as(C.POINTER(C.c_double)),
+               raw.ctypes.data_as(C.POINTER(C.c_double)), cost.ctypes.data_as(C.POINTER(C.c_double)), C.byref(ev),
+               None)
+        self.last_raw_poses = raw  # before the key curves store them
         return poses, cost, ev.value
 
     def track(self, frames, poses, method=0, n_particles=64, n_iter=30, w=0.7298, c1=1.4962, c2=1.4962, lo=-6.0,
@@ -334,6 +343,22 @@ class Engine:
                cost.ctypes.data_as(C.POINTER(C.c_double)), C.byref(ev), None)
         self.rads = list(frames[-1] if dframe > 0 else frames[0])  # the views' radiographs now
         return out, cost, ev.value
+
+    def optimize_curves(self, curves, frame, n_frames, method=0, n_particles=64, n_iter=30, w=0.7298, c1=1.4962,
+                        c2=1.4962, lo=-6.0, hi=6.0, seed=1, offsets=(0.1,) * 6, ftol=1e-3, repeats=1, guess=1, dframe=1,
+                        max_stall=0):
+        """Tracker::optimize at `frame` against each bone's PoseCurve
+        (asc_engine_optimize_curves): the guess and the optimized poses are
+        inserted into the curves.  Returns (costs per bone, evaluations)."""
+        nb = len(self.scene.volumes)
+        hs = (C.c_void_p * nb)(*[c.handle for c in curves])
+        p = L.TrackParams(L.OptParams(method, n_particles, n_iter, w, c1, c2, lo, hi, seed, (C.c_double * 6)(*offsets),
+                                      ftol, max_stall), repeats, guess, dframe, None)
+        cost = np.zeros(nb)
+        ev = C.c_longlong()
+        L.call("asc_engine_optimize_curves", self.handle, hs, int(frame), int(n_frames), C.byref(p),
+               cost.ctypes.data_as(C.POINTER(C.c_double)), C.byref(ev), None)
+        return cost, ev.value
 
     def render_drr(self, view, poses, viewport=None):
         """View::renderDrr: all bones at `poses` (n_bones x 6), merged and

@@ -212,3 +212,31 @@ ASC_API int asc_pose_curve_eval(asc_pose_curve c, int frame, double xyzypr[6])
   quat_to_ypr(c->q.eval(frame), xyzypr + 3);
   return ASC_OK;
 }
+
+// The 4 x 4 column-major matrix of a pose (CoordFrame::from_xyzypr then
+// to_matrix, CoordFrame.cpp:100-108, :203-221) and back (from_matrix then
+// to_xyzypr, :191-201, :177-189): the tracking-file conversions.
+ASC_API int asc_pose_to_matrix(const double xyzypr[6], double m[16])
+{
+  if (!xyzypr || !m) return ASC_ERR_ARG;
+  double f[12];
+  frame_from_xyzypr(xyzypr, f);
+  for (int c = 0; c < 3; ++c) {
+    for (int r = 0; r < 3; ++r) m[4 * c + r] = f[3 * c + r];
+    m[4 * c + 3] = 0.0;
+  }
+  for (int r = 0; r < 3; ++r) m[12 + r] = f[9 + r];
+  m[15] = 1.0;
+  return ASC_OK;
+}
+
+ASC_API int asc_pose_from_matrix(const double m[16], double xyzypr[6])
+{
+  if (!xyzypr || !m) return ASC_ERR_ARG;
+  double f[12];
+  for (int c = 0; c < 3; ++c)
+    for (int r = 0; r < 3; ++r) f[3 * c + r] = m[4 * c + r];
+  for (int r = 0; r < 3; ++r) f[9 + r] = m[12 + r];
+  frame_to_xyzypr(f, xyzypr);
+  return ASC_OK;
+}

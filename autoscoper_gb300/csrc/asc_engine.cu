@@ -72,6 +72,7 @@ struct BoneDev {
   double pivot[12], pivot_inv[12], base[6];
   float step[MAX_VIEWS], scale[MAX_VIEWS], cutoff_raw[MAX_VIEWS];
   const uint8_t* occ[MAX_VIEWS];  // empty-cell grids per view's cutoff
+  int visible;                    // RayCaster::setVisible: a hidden volume renders zeros
 };
 
 struct SceneDev {
@@ -187,8 +188,9 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
         df_split((double)r.vp[2] / (double)w, r.sx[0], r.sx[1]);
         df_split((double)r.vp[3] / (double)h, r.sy[0], r.sy[1]);
       }
-      if (w == 0 || h == 0) {
-        // an empty crop: the degenerate NCC (1e5), or the SAD of no pixels
+      if (w == 0 || h == 0 || !B.visible) {
+        // an empty crop, or the all-zero DRR of a hidden volume (RayCaster.cpp:131-134),
+        // whose mask is empty: the degenerate NCC (1e5), or the SAD of no pixels
         vc = sc->cf_model ? 0.0 : 1.0 - 1e5;
       } else {
         r.ok = 1;
@@ -1233,6 +1235,7 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
     memcpy(B.pivot, bones[i].pivot, sizeof B.pivot);
     frame_inverse(B.pivot, B.pivot_inv);
     set_base(B, bones[i].base_pose);
+    B.visible = 1;
     for (int v = 0; v < n_views; ++v) {
       B.step[v] = bones[i].step[v];
       B.scale[v] = bones[i].step[v] * vh->dev.norm / bones[i].intensity[v];
@@ -1324,14 +1327,26 @@ ASC_API int asc_engine_set_base_pose(asc_engine e, int bone, const double xyzypr
   return ASC_OK;
 }
 
+ASC_API int asc_engine_set_visible(asc_engine e, int bone, int visible)
+{
+  if (!e || bone < 0 || bone >= e->n_bones) return ASC_ERR_ARG;
+  e->host.bones[bone].visible = visible ? 1 : 0;
+  Gate g(device_gate());
+  ASC_CUDA(cudaMemcpy(&e->dev->bones[bone].visible, &e->host.bones[bone].visible, sizeof(int),
+                      cudaMemcpyHostToDevice));
+  return ASC_OK;
+}
+
 ASC_API int asc_engine_set_radiograph(asc_engine e, int view, asc_image rad)
 {
   if (!e || !rad || view < 0 || view >= e->n_views) return ASC_ERR_ARG;
   ViewDev& d = e->host.views[view];
   int bps;
-  d.rad = image_data(rad, &d.rad_w, &d.rad_h, &bps);
+  const void* data = image_data(rad, &d.rad_w, &d.rad_h, &bps);
   if (bps == 32) return ASC_ERR_ARG;
+  d.rad = data;
   d.rad_bps = bps;
+  e->vdesc[view].radiograph = rad;  // the plain path and the image exports read it there
   Gate g(device_gate());
   ASC_CUDA(cudaMemcpy(&e->dev->views[view], &d, sizeof d, cudaMemcpyHostToDevice));
   return ASC_OK;
@@ -1558,6 +1573,19 @@ static void view_matrix(const ViewDev& V, const BoneDev& B, const double* xyzypr
   fold_matrix(imv16, B.inv_scale, B.inv_trans, m);
 }
 
+// RayCaster::render (RayCaster.cpp:123-143) of one bone into `out`: zeros
+// for a hidden volume.
+static int render_bone(const BoneDev& B, const asc_bone_desc& BD, int v, const float* m, const float* vpf,
+                       float* out, int w, int h, cudaStream_t s)
+{
+  if (!B.visible) {
+    ASC_CUDA(cudaMemsetAsync(out, 0, (size_t)w * h * sizeof(float), s));
+    return ASC_OK;
+  }
+  return raycast_launch(B.vol, g_empty_skip ? B.occ[v] : nullptr, m, vpf, BD.step[v], BD.intensity[v], BD.cutoff[v],
+                        out, w, h, s);
+}
+
 ASC_API int asc_engine_eval_plain(asc_engine e, int n, const int* bone, const double* manip, double* cost,
                                   double* view_cost, void* stream)
 {
@@ -1599,8 +1627,7 @@ ASC_API int asc_engine_eval_plain(asc_engine e, int n, const int* bone, const do
           vc = S_.cf_model ? 0.0 : 1.0 - 1e5;
         } else {
           float vpf[4] = {(float)vp[0], (float)vp[1], (float)vp[2], (float)vp[3]};
-          int rc = raycast_launch(B.vol, g_empty_skip ? B.occ[v] : nullptr, m, vpf, BD.step[v], BD.intensity[v],
-                                  BD.cutoff[v], e->p_drr, w, h, s);
+          int rc = render_bone(B, BD, v, m, vpf, e->p_drr, w, h, s);
           float *d = e->p_drr, *o = e->p_tmp;
           if (!rc) rc = chain_plain(VD.drr_filters, VD.n_drr_filters, d, o, w, h, s);
           // the DRR chain ping-pongs p_drr/p_tmp and leaves one of them free (o);
@@ -1676,8 +1703,8 @@ void compose_pose(const BoneDev& B, const double* base6, const double* manip, do
 
 }  // namespace
 
-ASC_API int asc_engine_optimize_frame(asc_engine e, const asc_opt_params* p, double* pose_out, double* cost_out,
-                                      long long* evals_out, void* stream)
+ASC_API int asc_engine_optimize_frame_ex(asc_engine e, const asc_opt_params* p, double* pose_out, double* raw_out,
+                                         double* cost_out, long long* evals_out, void* stream)
 {
   if (!e || !p || !pose_out) return ASC_ERR_ARG;
   const int nb = e->n_bones;
@@ -1748,10 +1775,18 @@ ASC_API int asc_engine_optimize_frame(asc_engine e, const asc_opt_params* p, dou
     rc = asc_engine_set_base_pose(e, b, st);
     if (rc) return rc;
     for (int j = 0; j < 6; ++j) pose_out[6 * b + j] = st[j];
+    if (raw_out)
+      for (int j = 0; j < 6; ++j) raw_out[6 * b + j] = np[j];
     if (cost_out) cost_out[b] = take ? fin[b] : init[b];
   }
   if (evals_out) *evals_out = ctx.evals;
   return ASC_OK;
+}
+
+ASC_API int asc_engine_optimize_frame(asc_engine e, const asc_opt_params* p, double* pose_out, double* cost_out,
+                                      long long* evals_out, void* stream)
+{
+  return asc_engine_optimize_frame_ex(e, p, pose_out, nullptr, cost_out, evals_out, stream);
 }
 
 ASC_API int asc_keycurve_store(const double pose[6], double out[6])
@@ -1811,6 +1846,53 @@ ASC_API int asc_engine_track(asc_engine e, int n_frames, const asc_image* rads, 
   return ASC_OK;
 }
 
+ASC_API int asc_engine_optimize_curves(asc_engine e, const asc_pose_curve* curves, int frame, int n_frames,
+                                       const asc_track_params* tp, double* costs, long long* evals_out, void* stream)
+{
+  if (!e || !curves || !tp || tp->repeats < 0 || tp->guess < 0 || frame < 0 || frame >= n_frames)
+    return ASC_ERR_ARG;
+  const int nb = e->n_bones, d = tp->dframe;
+  for (int b = 0; b < nb; ++b)
+    if (!curves[b]) return ASC_ERR_ARG;
+  // initial guess (Tracker.cpp:386-426), written into the curves at `frame`
+  const int behind = d > 0 ? frame : n_frames - frame - 1;
+  for (int b = 0; b < nb; ++b) {
+    double p1[6], p2[6], g[6];
+    if (tp->guess == 2 && behind > 1) {
+      double a[12], c[12], x[12];
+      asc_pose_curve_eval(curves[b], frame - 2 * d, p1);
+      asc_pose_curve_eval(curves[b], frame - d, p2);
+      frame_from_xyzypr(p1, a);
+      frame_from_xyzypr(p2, c);
+      frame_linear_extrap(a, c, x);
+      frame_to_xyzypr(x, g);
+      asc_pose_curve_insert(curves[b], frame, g, ASC_CURVE_ALL);
+    } else if (tp->guess == 1 && behind > 0) {
+      asc_pose_curve_eval(curves[b], frame - d, g);
+      asc_pose_curve_insert(curves[b], frame, g, ASC_CURVE_ALL);
+    }
+  }
+  // repeats (Tracker.cpp:428-572): from the curves' pose at the frame, the
+  // optimized pose inserted back
+  long long evals = 0;
+  std::vector<double> stored(6 * nb), raw(6 * nb);
+  for (int r = 0; r < tp->repeats; ++r) {
+    for (int b = 0; b < nb; ++b) {
+      double base[6];
+      asc_pose_curve_eval(curves[b], frame, base);
+      int rc = asc_engine_set_base_pose(e, b, base);
+      if (rc) return rc;
+    }
+    long long ev = 0;
+    int rc = asc_engine_optimize_frame_ex(e, &tp->opt, stored.data(), raw.data(), costs, &ev, stream);
+    if (rc) return rc;
+    evals += ev;
+    for (int b = 0; b < nb; ++b) asc_pose_curve_insert(curves[b], frame, raw.data() + 6 * b, ASC_CURVE_ALL);
+  }
+  if (evals_out) *evals_out = evals;
+  return ASC_OK;
+}
+
 // ---------------------------------------------------------------- images
 ASC_API int asc_engine_render_drr(asc_engine e, int view, const double* poses, const double* viewport, float* out,
                                   void* stream)
@@ -1834,6 +1916,7 @@ ASC_API int asc_engine_render_drr(asc_engine e, int view, const double* poses, c
     const asc_bone_desc& BD = e->bdesc[b];
     float m[12];
     view_matrix(V, B, poses + 6 * b, m);
+    if (!B.visible) continue;  // its zeros leave the merge unchanged
     int rc = raycast_launch(B.vol, g_empty_skip ? B.occ[view] : nullptr, m, vpf, BD.step[view], BD.intensity[view],
                             BD.cutoff[view], e->p_drr, w, h, s);
     if (!rc) rc = asc_merge(e->p_mask, e->p_drr, e->p_mask, w, h, s);
@@ -1862,8 +1945,7 @@ ASC_API int asc_engine_image_data(asc_engine e, int view, int bone, const double
   const float vpf[4] = {(float)vp[0], (float)vp[1], (float)vp[2], (float)vp[3]};
   float m[12];
   view_matrix(V, B, pose, m);
-  int rc = raycast_launch(B.vol, g_empty_skip ? B.occ[view] : nullptr, m, vpf, BD.step[view], BD.intensity[view],
-                          BD.cutoff[view], e->p_drr, w, h, s);
+  int rc = render_bone(B, BD, view, m, vpf, e->p_drr, w, h, s);
   float *d = e->p_drr, *o = e->p_tmp;
   if (!rc) rc = chain_plain(VD.drr_filters, VD.n_drr_filters, d, o, w, h, s);
   if (!rc) rc = asc_rad_render(VD.radiograph, V.ipf, vpf, e->p_rad, w, h, s);

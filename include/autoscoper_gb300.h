@@ -235,6 +235,10 @@ int asc_engine_create(int n_views, const asc_view_desc *views, int n_bones, cons
 int asc_engine_destroy(asc_engine e);
 int asc_engine_set_base_pose(asc_engine e, int bone, const double xyzypr[6]);
 int asc_engine_set_radiograph(asc_engine e, int view, asc_image radiograph);
+/* RayCaster::setVisible for one bone in every view (the volume visibility
+ * of AutoscoperMainWindow::setVolumeVisibility): a hidden bone renders an
+ * all-zero DRR, so its views score the empty-mask cost. */
+int asc_engine_set_visible(asc_engine e, int bone, int visible);
 /* Scores n candidates: bone[i] and manip[6*i] (xyz mm + axis-angle degrees,
  * CoordFrame::from_xyzAxis_angle).  cost_dev (device, n doubles) receives
  * minimizationFunc's value; view_cost_dev (optional, n*n_views) the per-view
@@ -313,6 +317,11 @@ typedef struct {
 } asc_opt_params;
 int asc_engine_optimize_frame(asc_engine e, const asc_opt_params *params, double *pose_out, double *cost_out,
                               long long *evals_out, void *stream);
+/* asc_engine_optimize_frame that also returns, per bone, the pose before the
+ * key curves store it (raw_out, 6 per bone: the xyzypr Tracker::optimize
+ * inserts into its curves, Tracker.cpp:558-571). */
+int asc_engine_optimize_frame_ex(asc_engine e, const asc_opt_params *params, double *pose_out, double *raw_out,
+                                 double *cost_out, long long *evals_out, void *stream);
 
 /* View::renderDrr (View.cpp:201-231) on an engine's view: the DRRs of all
  * bones at poses (n_bones x 6 xyzypr) over `viewport` (NULL: the whole
@@ -356,6 +365,11 @@ int asc_pose_curve_insert(asc_pose_curve c, int frame, const double xyzypr[6], i
 int asc_pose_curve_erase(asc_pose_curve c, int frame, int mask);
 int asc_pose_curve_keys(asc_pose_curve c, int frame, int *mask);
 int asc_pose_curve_eval(asc_pose_curve c, int frame, double xyzypr[6]);
+/* A pose as the 4 x 4 column-major matrix of its CoordFrame (from_xyzypr
+ * then to_matrix, CoordFrame.cpp:100-108, :203-221) and back (from_matrix
+ * then to_xyzypr, :177-201): the tracking files' matrix form. */
+int asc_pose_to_matrix(const double xyzypr[6], double m[16]);
+int asc_pose_from_matrix(const double m[16], double xyzypr[6]);
 
 /* A sequence of Tracker::optimize calls (Tracker.cpp:337-580), frames in
  * order (dframe +1) or in reverse (dframe -1).  Per frame: the views take
@@ -377,6 +391,18 @@ typedef struct {
 } asc_track_params;
 int asc_engine_track(asc_engine e, int n_frames, const asc_image *rads, const asc_track_params *params,
                      double *poses, double *costs, long long *evals_out, void *stream);
+
+/* Tracker::optimize (Tracker.cpp:337-580) at one frame against each bone's
+ * pose curves (curves: one asc_pose_curve per bone), with the views'
+ * radiographs of that frame already set: the initial guess (params->guess 2:
+ * CoordFrame::linear_extrap of the curves at frame - 2 dframe and
+ * frame - dframe, when more than one frame lies behind in the dframe
+ * direction; 1: the curves at frame - dframe, when one does) inserted at the
+ * frame, then params->repeats times asc_engine_optimize_frame from the
+ * curves' pose at the frame, the optimized pose inserted back.  n_frames:
+ * the trial's frame count; keyed is not used.  costs (optional): per bone. */
+int asc_engine_optimize_curves(asc_engine e, const asc_pose_curve *curves, int frame, int n_frames,
+                               const asc_track_params *params, double *costs, long long *evals_out, void *stream);
 
 /* Reference-sequential PSO on the host (PSO.cpp:198-295, asynchronous gBest,
  * glibc rand() after srand(seed), omega 0.8 * 0.9^epoch, c1 = c2 = 1.5),

@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from autoscoper_gb300 import formats as F, geometry as G, scene as S
+import trial_files
 
 SAMPLE = "/root/reference/sample_data"
 
@@ -54,31 +55,10 @@ def test_volume_from_pages_and_pivot(tmp_path):
     assert np.allclose(pv[9:12], want)
 
 
-def _write_mayacam2(path, frame, W, H, cx, cy, fx, fy):
-    """The file read_mayacam2 turns into this camera (its conversion run
-    backwards)."""
-    R = np.asarray(frame[:9]).reshape(3, 3).copy()   # rows = stored columns of CoordFrame
-    t = np.asarray(frame[9:12]).copy()
-    R[0, :] = -R[0, :]
-    R[1, :] = -R[1, :]
-    t_wc = -(R @ t)  # R is orthonormal: undo t' = -R^T t (as rows)
-    Rf = R.T.copy()
-    Rf[:, 0] = -Rf[:, 0]
-    Rf[:, 2] = -Rf[:, 2]
-    t_wc = np.array([-t_wc[0], t_wc[1], -t_wc[2]])
-    K = np.array([[fx, 0, 0], [0, fy, 0], [cx, (H - 1) - cy, 1.0]])
-    lines = ["image size", f"{W},{H}", "", "camera matrix"]
-    lines += [",".join(repr(float(K[j, i])) for j in range(3)) for i in range(3)]
-    lines += ["", "rotation"]
-    lines += [",".join(repr(float(Rf[j, i])) for j in range(3)) for i in range(3)]
-    lines += ["", "translation"] + [repr(float(x)) for x in t_wc]
-    open(path, "w").write("\n".join(lines) + "\n")
-
-
 def test_mayacam2_round_trip_and_vtk(tmp_path):
     frame = G.look_at_frame((420.0, -80.0, 35.0), (0.0, 5.0, -3.0), (0.0, 0.0, 1.0))
     p = str(tmp_path / "cam.txt")
-    _write_mayacam2(p, frame, 1024, 960, 515.5, 470.25, 4000.0, 4010.0)
+    trial_files.write_mayacam2(p, frame, 1024, 960, 515.5, 470.25, 4000.0, 4010.0)
     cam = F.read_camera(p)
     assert np.allclose(cam.frame, frame, atol=1e-12)
     assert (cam.width, cam.height, cam.cx, cam.cy, cam.fx, cam.fy) == (1024, 960, 515.5, 470.25, 4000.0, 4010.0)
@@ -117,26 +97,9 @@ def test_vie_settings(tmp_path):
     assert vs.drr_filters[1].radius == 2.0 and vs.drr_filters[1].contrast == 1.2
 
 
-def _synthetic_trial(tmp_path):
-    sc = S.make_scene([(24, 28, 32)], 1.0, (64, 64), 1.6, filters="sobel", seed=2)
-    F.write_tiff(str(tmp_path / "bone.tif"), list(sc.volumes[0].data), "lzw")
-    for i, v in enumerate(sc.views):
-        c = v.camera
-        _write_mayacam2(str(tmp_path / f"cam{i}.txt"), c.frame, c.width, c.height, c.cx, c.cy, c.fx, c.fy)
-        os.makedirs(tmp_path / f"video{i}", exist_ok=True)
-        for f in range(2):
-            F.write_tiff(str(tmp_path / f"video{i}" / f"frame_{f:03d}.tif"),
-                         [np.full((64, 64), 30000 + 100 * f, np.uint16)], "packbits")
-    cfg = tmp_path / "trial.cfg"
-    cfg.write_text("# synthetic trial\nVersion 1.1\nmayaCam_csv cam0.txt\nmayaCam_csv cam1.txt\n"
-                   "CameraRootDir video0\nCameraRootDir video1\nVolumeFile bone.tif\nVoxelSize 1 1 1\n"
-                   "VolumeFlip 0 0 0\nRenderResolution 64 64\nOptimizationOffsets 0.2 0.2 0.2 0.1 0.1 0.1\n")
-    return sc, str(cfg)
-
-
 def test_cfg_and_trial_to_scene(tmp_path):
     from oracle import oracle as O
-    sc, cfg = _synthetic_trial(tmp_path)
+    sc, cfg = trial_files.synthetic_trial(tmp_path)
     t = F.read_cfg(cfg)
     assert t.version == (1, 1) and (t.render_width, t.render_height) == (64, 64)
     assert t.offsets == (0.2, 0.2, 0.2, 0.1, 0.1, 0.1) and t.flips == [(0, 0, 0)]
@@ -174,7 +137,7 @@ def test_trial_from_files_on_the_engine(tmp_path):
     """A trial read from its files scores on the engine as on the oracle."""
     from autoscoper_gb300 import api
     from oracle import oracle as O
-    sc, cfg = _synthetic_trial(tmp_path)
+    sc, cfg = trial_files.synthetic_trial(tmp_path)
     loaded = F.load_trial(cfg, frame=0)
     loaded.poses = [np.asarray(sc.truth[0], np.float32)]
     tr = O.Tracker(loaded)
