@@ -531,32 +531,36 @@ __device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup
     az = __fadd_rn(Z, -__fadd_rn(tz, -M));
     return min(__float_as_uint(tz) * pxy + __float_as_uint(ty) * px + __float_as_uint(tx) + i_base, imax);
   };
-  float ax, ay, az;
-  Taps<STORE> cur = fetch_taps<STORE>(P, locate(j, ax, ay, az), px, pxy);
-  for (int k = js; k <= je; ++k) {
-    // the next sample's loads go out before this sample's arithmetic (after
-    // the last sample they re-read clamped, in-bounds words)
-    j += 1.0f;
-    float bx, by, bz;
-    const Taps<STORE> nxt = fetch_taps<STORE>(P, locate(j, bx, by, bz), px, pxy);
-    const float e00 = lerp_tap<STORE>(cur, 0, ax);
-    const float e10 = lerp_tap<STORE>(cur, 1, ax);
-    const float e01 = lerp_tap<STORE>(cur, 2, ax);
-    const float e11 = lerp_tap<STORE>(cur, 3, ax);
-    const float f0 = fmaf(ay, e10 - e00, e00);
-    const float f1 = fmaf(ay, e11 - e01, e01);
-    const float s = fmaf(az, f1 - f0, f0);
-    if (s > cutoff_raw) {
-      const float y = s - comp;
+  // one sample's trilinear value from its taps, added when above the cutoff
+  auto accumulate = [&](const Taps<STORE>& t, float wx, float wy, float wz) {
+    const float e00 = lerp_tap<STORE>(t, 0, wx);
+    const float e10 = lerp_tap<STORE>(t, 1, wx);
+    const float e01 = lerp_tap<STORE>(t, 2, wx);
+    const float e11 = lerp_tap<STORE>(t, 3, wx);
+    const float f0 = fmaf(wy, e10 - e00, e00);
+    const float f1 = fmaf(wy, e11 - e01, e01);
+    const float v = fmaf(wz, f1 - f0, f0);
+    if (v > cutoff_raw) {
+      const float y = v - comp;
       const float tt = acc + y;
       comp = (tt - acc) - y;
       acc = tt;
     }
-    cur = nxt;
-    ax = bx;
-    ay = by;
-    az = bz;
+  };
+  // Two samples per iteration over two tap sets A and B, each sample's loads
+  // issued one sample ahead of its arithmetic (after the last sample they
+  // re-read clamped, in-bounds words); the samples add in order.
+  float ax, ay, az, bx, by, bz;
+  Taps<STORE> A = fetch_taps<STORE>(P, locate(j, ax, ay, az), px, pxy);
+  int k = js;
+  for (; k < je; k += 2) {
+    const Taps<STORE> B = fetch_taps<STORE>(P, locate(j + 1.0f, bx, by, bz), px, pxy);
+    accumulate(A, ax, ay, az);
+    j += 2.0f;
+    A = fetch_taps<STORE>(P, locate(j, ax, ay, az), px, pxy);
+    accumulate(B, bx, by, bz);
   }
+  if (k == je) accumulate(A, ax, ay, az);
   return make_float2(acc, comp);
 }
 
