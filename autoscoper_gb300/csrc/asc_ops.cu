@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(RB) k_hdist_sad(const float* __restrict__ f, c
   }
 }
 
-// Occupancy of 8^3-voxel cells (OCC, OCC_LO, OCC_HI in asc_march.cuh): one
+// Occupancy of OCC^3-voxel cells (OCC, OCC_LO, OCC_HI in asc_march.cuh): one
 // thread per cell takes the maximum over the cell and its apron.
 template <int STORE>
 __global__ void k_occupancy(DevVolume V, float cutoff_raw, uint8_t* __restrict__ occ)
