@@ -60,7 +60,7 @@ struct asc_volume_host {
 void build_occupancy(const DevVolume& V, float cutoff_raw, uint8_t* occ, cudaStream_t s);
 inline size_t occupancy_cells(const DevVolume& V)
 {
-  return (size_t)((V.nx + OCC - 1) / OCC) * ((V.ny + OCC - 1) / OCC) * ((V.nz + OCC - 1) / OCC);
+  return (size_t)occ_dim(V.nx) * occ_dim(V.ny) * occ_dim(V.nz);
 }
 
 // Global switches (asc_set_option).

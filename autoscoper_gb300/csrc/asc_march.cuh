@@ -190,6 +190,11 @@ __device__ __forceinline__ float lerp_tap(const Taps<STORE>& t, int k, float a)
 // exactly nothing to the DRR (RayCaster_kernels.cu:189); the march skips it.
 constexpr int OCC = 4;  // 4^3 cells: 36 % fewer samples marched than with 8^3, for a longer walk
 constexpr int OCC_LO = 1, OCC_HI = 2;  // apron voxels below and above a cell
+// The grid holds OCC_PAD cells of margin on every side (cells -2 .. b + 1 of
+// an axis of b cells), so that a walk, whose cells stay within one of the
+// box's, indexes it without clamping.
+constexpr int OCC_PAD = 2;
+__host__ __device__ __forceinline__ int occ_dim(int n) { return (n + OCC - 1) / OCC + 2 * OCC_PAD; }
 
 
 // ---- double-float arithmetic: a value is the unevaluated sum h + l of two
@@ -368,9 +373,10 @@ constexpr int REBASE = ASC_REBASE;
 struct CellWalk {
   float tx, ty, tz;     // next crossing per axis (sample index; +inf if none)
   float dtx, dty, dtz;  // samples between crossings
-  int cx, cy, cz;       // current cell (unclamped)
-  int sx, sy, sz;       // cell index change per crossing
-  int bx, by, bz;       // grid size in cells
+  int cell;             // the current cell's index in the padded grid
+  int ix, iy, iz;       // index change per crossing of each axis
+  unsigned last;        // the grid's last index (a bound no walk reaches)
+  int steps;            // crossings a ray can make through the grid
 };
 
 __device__ __forceinline__ void walk_axis(float C, float dC, float kf, float& t, float& dt, int& c, int& st)
@@ -397,12 +403,17 @@ __device__ __forceinline__ CellWalk cell_walk(const DevVolume& V, const RaySetup
 {
   CellWalk w;
   const float kf = (float)k;
-  walk_axis(r.X.h, r.dX.h, kf, w.tx, w.dtx, w.cx, w.sx);
-  walk_axis(r.Y.h, r.dY.h, kf, w.ty, w.dty, w.cy, w.sy);
-  walk_axis(r.Z.h, r.dZ.h, kf, w.tz, w.dtz, w.cz, w.sz);
-  w.bx = (V.nx + OCC - 1) / OCC;
-  w.by = (V.ny + OCC - 1) / OCC;
-  w.bz = (V.nz + OCC - 1) / OCC;
+  int cx, cy, cz, sx, sy, sz;
+  walk_axis(r.X.h, r.dX.h, kf, w.tx, w.dtx, cx, sx);
+  walk_axis(r.Y.h, r.dY.h, kf, w.ty, w.dty, cy, sy);
+  walk_axis(r.Z.h, r.dZ.h, kf, w.tz, w.dtz, cz, sz);
+  const int px = occ_dim(V.nx), py = occ_dim(V.ny), pz = occ_dim(V.nz);
+  w.cell = ((cz + OCC_PAD) * py + (cy + OCC_PAD)) * px + (cx + OCC_PAD);
+  w.ix = sx;
+  w.iy = sy * px;
+  w.iz = sz * px * py;
+  w.last = (unsigned)(px * py * pz - 1);
+  w.steps = 2 * (px + py + pz);
   return w;
 }
 
@@ -424,7 +435,7 @@ struct WalkState {
 template <class Emit>
 __device__ __forceinline__ bool walk_segments(CellWalk& w, const uint8_t* __restrict__ occ, WalkState& s, Emit&& emit)
 {
-  int steps = 2 * (w.bx + w.by + w.bz) + 8;
+  int steps = w.steps;
   while (s.k <= s.kend) {
     int ke = s.kend;
     bool full = true;
@@ -432,9 +443,7 @@ __device__ __forceinline__ bool walk_segments(CellWalk& w, const uint8_t* __rest
     if (occ && steps > 0) {
       tn = fminf(w.tx, fminf(w.ty, w.tz));
       if (tn < (float)s.kend) ke = (int)floorf(tn);
-      const int cx = min(max(w.cx, 0), w.bx - 1), cy = min(max(w.cy, 0), w.by - 1),
-                cz = min(max(w.cz, 0), w.bz - 1);
-      full = __ldg(occ + (cz * w.by + cy) * w.bx + cx) != 0;
+      full = __ldg(occ + min((unsigned)w.cell, w.last)) != 0;
       --steps;
     }
     if (ke >= s.k) {
@@ -460,13 +469,13 @@ __device__ __forceinline__ bool walk_segments(CellWalk& w, const uint8_t* __rest
       s.k = ke + 1;
     }
     if (tn == w.tx) {
-      w.cx += w.sx;
+      w.cell += w.ix;
       w.tx += w.dtx;
     } else if (tn == w.ty) {
-      w.cy += w.sy;
+      w.cell += w.iy;
       w.ty += w.dty;
     } else {
-      w.cz += w.sz;
+      w.cell += w.iz;
       w.tz += w.dtz;
     }
   }

@@ -390,15 +390,16 @@ __global__ void __launch_bounds__(RB) k_hdist_sad(const float* __restrict__ f, c
   }
 }
 
-// Occupancy of OCC^3-voxel cells (OCC, OCC_LO, OCC_HI in asc_march.cuh): one
-// thread per cell takes the maximum over the cell and its apron.
+// Occupancy of OCC^3-voxel cells (OCC, OCC_LO, OCC_HI, OCC_PAD in
+// asc_march.cuh), margin cells included: one thread per cell takes the
+// maximum over the cell and its apron (voxels outside the volume are 0).
 template <int STORE>
 __global__ void k_occupancy(DevVolume V, float cutoff_raw, uint8_t* __restrict__ occ)
 {
-  const int bx = (V.nx + OCC - 1) / OCC, by = (V.ny + OCC - 1) / OCC, bz = (V.nz + OCC - 1) / OCC;
+  const int px = occ_dim(V.nx), py = occ_dim(V.ny), pz = occ_dim(V.nz);
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= bx * by * bz) return;
-  const int cx = c % bx, cy = (c / bx) % by, cz = c / (bx * by);
+  if (c >= px * py * pz) return;
+  const int cx = c % px - OCC_PAD, cy = (c / px) % py - OCC_PAD, cz = c / (px * py) - OCC_PAD;
   float mx = -1.0f;
   const int lo = -OCC_LO, hi = OCC + OCC_HI;
   for (int z = max(cz * OCC + lo, 0); z < min(cz * OCC + hi, V.nz); ++z)

@@ -38,11 +38,11 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
   DevVolume V{pairs.data(), nx, ny, nz, px, pxy, storage, 1.0f / 65535.0f};
   const float cut = cutoff / V.norm;
   // occupancy as k_occupancy builds it
-  const int bx = (nx + OCC - 1) / OCC, by = (ny + OCC - 1) / OCC, bz = (nz + OCC - 1) / OCC;
+  const int bx = occ_dim(nx), by = occ_dim(ny), bz = occ_dim(nz);
   std::vector<uint8_t> occ((size_t)bx * by * bz);
-  for (int cz = 0; cz < bz; ++cz)
-    for (int cy = 0; cy < by; ++cy)
-      for (int cx = 0; cx < bx; ++cx) {
+  for (int cz = -OCC_PAD; cz < bz - OCC_PAD; ++cz)
+    for (int cy = -OCC_PAD; cy < by - OCC_PAD; ++cy)
+      for (int cx = -OCC_PAD; cx < bx - OCC_PAD; ++cx) {
         float mx = -1.0f;
         for (int z = std::max(cz * OCC - OCC_LO, 0); z < std::min(cz * OCC + OCC + OCC_HI, nz); ++z)
           for (int y = std::max(cy * OCC - OCC_LO, 0); y < std::min(cy * OCC + OCC + OCC_HI, ny); ++y)
@@ -52,7 +52,7 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
                                 : storage == ASC_STORE_F32 ? voxel_value<ASC_STORE_F32>(V, i)
                                                            : voxel_value<ASC_STORE_U16>(V, i));
             }
-        occ[((size_t)cz * by + cy) * bx + cx] = mx > cut ? 1 : 0;
+        occ[((size_t)(cz + OCC_PAD) * by + (cy + OCC_PAD)) * bx + (cx + OCC_PAD)] = mx > cut ? 1 : 0;
       }
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
