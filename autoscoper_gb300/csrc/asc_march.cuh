@@ -436,38 +436,38 @@ template <class Emit>
 __device__ __forceinline__ bool walk_segments(CellWalk& w, const uint8_t* __restrict__ occ, WalkState& s, Emit&& emit)
 {
   int steps = w.steps;
-  while (s.k <= s.kend) {
-    int ke = s.kend;
+  // tp: the cell's entry crossing; its first sample is floor(tp) + 1
+  const float kendf = (float)s.kend;
+  float tp = (float)s.k - 0.5f;
+  while (tp < kendf) {
     bool full = true;
     float tn = 3.0e38f;
     if (occ && steps > 0) {
       tn = fminf(w.tx, fminf(w.ty, w.tz));
-      if (tn < (float)s.kend) ke = (int)floorf(tn);
       full = __ldg(occ + min((unsigned)w.cell, w.last)) != 0;
       --steps;
     }
-    if (ke >= s.k) {
-      if (full) {
-        // add samples [a, ke] to the open block(s)
-        for (int a = s.k; a <= ke;) {
-          const int bb = a / REBASE, hi = min(ke, bb * REBASE + REBASE - 1);
-          if (s.pf >= 0 && s.pb != bb) {
-            if (!emit(s.pb * REBASE, s.pf - s.pb * REBASE, s.pl - s.pb * REBASE)) {
-              s.k = a;  // resume here; the walk state still describes this cell
-              return false;
-            }
-            s.pf = -1;
+    if (full) {
+      // add the cell's samples [a, ke] to the open block(s)
+      const int ke = tn < kendf ? (int)floorf(tn) : s.kend;
+      for (int a = (int)floorf(tp) + 1; a <= ke;) {
+        const int bb = (int)((unsigned)a / REBASE), hi = min(ke, bb * REBASE + REBASE - 1);
+        if (s.pf >= 0 && s.pb != bb) {
+          if (!emit(s.pb * REBASE, s.pf - s.pb * REBASE, s.pl - s.pb * REBASE)) {
+            s.k = a;  // resume here; the walk state still describes this cell
+            return false;
           }
-          if (s.pf < 0) {
-            s.pb = bb;
-            s.pf = a;
-          }
-          s.pl = hi;
-          a = hi + 1;
+          s.pf = -1;
         }
+        if (s.pf < 0) {
+          s.pb = bb;
+          s.pf = a;
+        }
+        s.pl = hi;
+        a = hi + 1;
       }
-      s.k = ke + 1;
     }
+    tp = tn;
     if (tn == w.tx) {
       w.cell += w.ix;
       w.tx += w.dtx;
@@ -479,6 +479,7 @@ __device__ __forceinline__ bool walk_segments(CellWalk& w, const uint8_t* __rest
       w.tz += w.dtz;
     }
   }
+  s.k = s.kend + 1;
   if (s.pf >= 0) {
     if (!emit(s.pb * REBASE, s.pf - s.pb * REBASE, s.pl - s.pb * REBASE)) return false;
     s.pf = -1;
