@@ -754,6 +754,9 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
     const int rx0 = tx0 - eh, ry0 = ty0 - eh;
     const Region g{rx0, ry0, E, r.w, r.h, rx0 >= 0 && ry0 >= 0 && rx0 + E <= r.w && ry0 + E <= r.h};
     const float* drr = b.drr + r.pix;
+    // reciprocals for the film-plane mapping of this crop's pixels
+    const float fw = (float)r.w, fh = (float)r.h;
+    const float rcp[4] = {__frcp_rn(fw), __frcp_rn(fh), __frcp_rn(V.ipf[2]), __frcp_rn(V.ipf[3])};
     // ---- DRR region; a region of zeros filters to zeros (every filter maps
     // 0 to 0), so its tile masks out entirely and adds nothing to the moments
     bool live;
@@ -783,7 +786,7 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
         const int lo = eh - V.h_rad, hi = eh + VT + V.h_rad;
         for_band(lo, hi, lo, hi, [&](int ry, int rx) {
           float val = 0.f, s, tt;
-          if ((g.in || inside(g, ry, rx)) && image_coords(V.ipf, r.vp, g.x0 + rx, g.y0 + ry, r.w, r.h, s, tt))
+          if ((g.in || inside(g, ry, rx)) && image_coords_r(V.ipf, r.vp, g.x0 + rx, g.y0 + ry, fw, fh, rcp, s, tt))
             val = 1.0f - bilinear(V.rad, V.rad_bps, V.rad_w, V.rad_h, s, tt);
           bufs[0][ry * E + rx] = val;
         });
@@ -807,7 +810,7 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
           float bg = 1.0f;
           if (V.bg && V.bg_thr >= 0.f) {
             float ss, tt;
-            bg = image_coords(V.ipf, r.vp, x, y, r.w, r.h, ss, tt)
+            bg = image_coords_r(V.ipf, r.vp, x, y, fw, fh, rcp, ss, tt)
                    ? (V.bg_thr <= bilinear(V.bg, 32, V.bg_w, V.bg_h, ss, tt) ? 1.0f : 0.0f)
                    : 0.0f;
           }
