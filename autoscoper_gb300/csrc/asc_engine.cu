@@ -761,14 +761,21 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
     // 0 to 0), so its tile masks out entirely and adds nothing to the moments
     bool live;
     {
+      // the region's words copied asynchronously (all in flight at once;
+      // zero-filled outside the image), then tested for a nonzero DRR
       const int lo = eh - V.h_drr, hi = eh + VT + V.h_drr;
-      bool nz = false;
       for_band(lo, hi, lo, hi, [&](int ry, int rx) {
-        const float d =
-            (g.in || inside(g, ry, rx)) ? __ldg(drr + (long long)(g.y0 + ry) * r.w + g.x0 + rx) : 0.f;
-        bufs[0][ry * E + rx] = d;
-        nz |= d != 0.f;
+        const bool in = g.in || inside(g, ry, rx);
+        const float* src = in ? drr + (long long)(g.y0 + ry) * r.w + g.x0 + rx : drr;
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(bufs[0] + ry * E + rx);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(dst), "l"(src), "r"(in ? 4 : 0)
+                     : "memory");
       });
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+      __syncthreads();
+      bool nz = false;
+      for_band(lo, hi, lo, hi, [&](int ry, int rx) { nz |= bufs[0][ry * E + rx] != 0.f; });
       live = __syncthreads_or(nz);
     }
     float s[6] = {0, 0, 0, 0, 0, 0}, c[3] = {0, 0, 0};
