@@ -198,7 +198,7 @@ __host__ __device__ __forceinline__ int occ_dim(int n) { return (n + OCC - 1) / 
 
 
 // ---- double-float arithmetic: a value is the unevaluated sum h + l of two
-// FP32 numbers (Dekker/Knuth error-free transformations with FMA), about 48
+// FP32 numbers (Dekker/Knuth error-free transformations with FMA), 44 to 48
 // significant bits.  Used once per ray so that sample positions match FP64.
 struct df {
   float h, l;
@@ -217,13 +217,15 @@ __device__ __forceinline__ df df_fast(float a, float b)  // requires |a| >= |b|
   return {s, __fadd_rn(b, -__fadd_rn(s, -a))};
 }
 
+// Sum with an exact sum of the high parts and the low parts added in FP32
+// (Dekker's addition): relative error ~2^-44 of the larger operand.  Every
+// use here needs absolute accuracy in coordinates and ray parameters whose
+// magnitudes are at most ~1e4 (voxels, samples): ~1e-9 at worst, far below
+// the FP32 rounding of the sample positions the march then uses.
 __device__ __forceinline__ df df_add(df a, df b)
 {
   df s = df_two_sum(a.h, b.h);
-  const df t = df_two_sum(a.l, b.l);
-  s.l = __fadd_rn(s.l, t.h);
-  s = df_fast(s.h, s.l);
-  s.l = __fadd_rn(s.l, t.l);
+  s.l = __fadd_rn(s.l, __fadd_rn(a.l, b.l));
   return df_fast(s.h, s.l);
 }
 
