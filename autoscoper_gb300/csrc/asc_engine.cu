@@ -317,17 +317,21 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
   __shared__ unsigned s_seg[NRAY * NBW]; // per segment slot: slot | js << 11 | je << 17
   __shared__ unsigned s_ord[NRAY * NBW]; // the segments, longest first
   __shared__ int s_cnt[REBASE];          // segments per length - 1, then placement cursors
-  __shared__ int s_tile, s_nseg, s_grab;
+  __shared__ int s_tile, s_nseg, s_grab, s_k;
   const unsigned FULL = 0xffffffffu;
   const int tid = threadIdx.x, lane = tid & 31;
   const int nv = sc->n_views;
   unsigned long long marched = 0, slots = 0;
   for (;;) {
-    if (tid == 0) s_tile = atomicAdd(&b.C->rnext, 1);
+    if (tid == 0) {
+      const int tl = atomicAdd(&b.C->rnext, 1);
+      s_tile = tl;
+      s_k = tl < b.C->rtiles ? find_iv(b.roff, b.C->n_iv, tl) : 0;
+    }
     __syncthreads();
     const int tile = s_tile;
     if (tile >= b.C->rtiles) break;
-    const int k = find_iv(b.roff, b.C->n_iv, tile);
+    const int k = s_k;
     const IV& r = b.iv[k];
     const int t = tile - b.roff[k];
     const int x = (t % r.rtx) * RTX + (tid % RTX), y = (t / r.rtx) * RTY + (tid / RTX);
@@ -730,7 +734,7 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
     k_view(const SceneDev* __restrict__ sc, Bufs b, double* __restrict__ cost, double* __restrict__ view_cost_out)
 {
   extern __shared__ float smem[];
-  __shared__ int s_tile;
+  __shared__ int s_tile, s_k;
   __shared__ bool s_last;
   __shared__ float red[8 * 6];
   __shared__ float wsh[32];
@@ -740,12 +744,15 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
   Moments* msh = (Moments*)smem;          // reused by the merge
   const int nv = sc->n_views;
   for (;;) {
-    if (threadIdx.x == 0) s_tile = atomicAdd(&b.C->fnext, 1);
+    if (threadIdx.x == 0) {
+      const int tl = atomicAdd(&b.C->fnext, 1);
+      s_tile = tl;
+      s_k = tl < b.C->ftiles ? find_iv(b.foff, b.C->n_iv, tl) : 0;
+    }
     __syncthreads();
-    const int tile = s_tile;
+    const int tile = s_tile, k = s_k;
     __syncthreads();
     if (tile >= b.C->ftiles) return;
-    const int k = find_iv(b.foff, b.C->n_iv, tile);
     const IV& r = b.iv[k];
     const int t = tile - b.foff[k];
     const int tx0 = (t % r.ftx) * VT, ty0 = (t / r.ftx) * VT;

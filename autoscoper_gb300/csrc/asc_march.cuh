@@ -388,12 +388,14 @@ __device__ __forceinline__ void walk_axis(float C, float dC, float kf, float& t,
   c = __float2int_rd(X * (1.0f / OCC));
   if (dC > 0.f) {  // decreasing: next plane at OCC * c
     st = -1;
-    dt = OCC / dC;
-    t = kf + (X - (float)(OCC * c)) / dC;
+    const float ri = __frcp_rn(dC);
+    dt = OCC * ri;
+    t = fmaf(X - (float)(OCC * c), ri, kf);
   } else if (dC < 0.f) {  // increasing: next plane at OCC * (c + 1)
     st = 1;
-    dt = -OCC / dC;
-    t = kf + (X - (float)(OCC * (c + 1))) / dC;
+    const float ri = __frcp_rn(dC);
+    dt = -OCC * ri;
+    t = fmaf(X - (float)(OCC * (c + 1)), ri, kf);
   } else {
     st = 0;
     dt = 3.0e38f;

@@ -414,8 +414,10 @@ def handle_message(session: Session, data: bytes, log=sys.stderr) -> Optional[by
             return b"\x11"
         print("Cannot handle message", file=log)
         return b"\x00"
-    except (SessionError, struct.error, UnicodeDecodeError, ValueError, OSError) as e:
-        print(f"message {t}: {e}", file=log)
+    except (SessionError, L.AscError, struct.error, UnicodeDecodeError, ValueError, OSError, IndexError) as e:
+        # a failed command answers 0 and the server keeps serving (the
+        # reference's window would have shown the error)
+        print(f"message {t}: {type(e).__name__}: {e}", file=log)
         return b"\x00"
 
 

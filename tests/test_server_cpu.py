@@ -124,6 +124,17 @@ def test_session_errors_answer_zero():
     assert SV.handle_message(Failing(), pack(6, 0, 0)) == b"\x00"
     assert SV.handle_message(Failing(), pack(14)) == b"\x00"
 
+    class LibFailing(Stub):
+        def __getattr__(self, name):
+            def f(*a):
+                from autoscoper_gb300 import _lib as L
+                raise L.AscError("asc_engine_eval_host", -3)
+            return f
+    import io
+    log = io.StringIO()
+    assert SV.handle_message(LibFailing(), pack(8, 0, *POSE), log) == b"\x00"
+    assert "asc_engine_eval_host" in log.getvalue()
+
 
 def _recv(sock, n):
     out = b""
