@@ -120,3 +120,48 @@ def test_track_sequence_follows_reference_orchestration():
                 want[f, b] = O.keycurve_store(_compose(sc, b, want[f, b], manip))
     assert evals > 0
     assert np.abs(got - want).max() <= 2e-5, np.abs(got - want).max()
+
+
+def test_optimize_curves_follow_tracker_optimize():
+    """asc_engine_optimize_curves frame by frame over four frames of a linear
+    motion (guess 2: linear extrapolation from frame 2 on, before that the
+    curve's own value; one repeat, simplex only) against
+    Tracker::optimize (Tracker.cpp:386-571) written out over the oracle's
+    pose curves (pinned to KeyCurve.hpp) and the same engine's costs: the
+    curves agree at every frame."""
+    from autoscoper_gb300 import _lib as L
+    from test_gpu_engine import make_targets
+    sc = _scene(29)
+    tr = O.Tracker(sc)
+    truth0 = [np.asarray(t, np.float64) for t in sc.truth]
+    step = np.array([0.25, -0.2, 0.1, 0.2, -0.1, 0.15])
+    images = []
+    for f in range(4):
+        sc.truth = [t + f * step for t in truth0]
+        make_targets(sc, tr)
+        images.append([api.DeviceImage(v.radiograph.copy()) for v in sc.views])
+    nb, nv = len(sc.volumes), len(sc.views)
+    eng, ref_eng = api.Engine(sc, max_items=64), api.Engine(sc, max_items=64)
+    curves, ocurves = [api.PoseCurve() for _ in range(nb)], [O.PoseCurves() for _ in range(nb)]
+    for b in range(nb):
+        curves[b].insert(0, np.asarray(sc.poses[b], np.float64))
+        ocurves[b].insert(0, np.asarray(sc.poses[b], np.float64))
+    for f in range(4):
+        for v in range(nv):
+            eng.set_radiograph(v, images[f][v])
+            ref_eng.set_radiograph(v, images[f][v])
+        cost, evals = eng.optimize_curves(curves, f, 4, method=1, repeats=1, guess=2, dframe=1)
+        assert evals > 0 and np.all(np.isfinite(cost))
+        for b in range(nb):
+            if f > 1:
+                x = O.frame_linear_extrap(O.frame_from_xyzypr(ocurves[b].eval(f - 2)),
+                                          O.frame_from_xyzypr(ocurves[b].eval(f - 1)))
+                ocurves[b].insert(f, O.frame_to_xyzypr(x))
+            base = ocurves[b].eval(f)  # at frame 1: the curve holds frame 0's key beyond it
+            ref_eng.set_base_pose(b, base)
+            ocurves[b].insert(f, _compose(sc, b, base, _simplex(ref_eng, b)))
+        for b in range(nb):
+            for g in range(f + 1):
+                assert np.abs(curves[b].eval(g) - ocurves[b].eval(g)).max() <= 2e-5, (f, b, g)
+    with pytest.raises(L.AscError):
+        eng.optimize_curves(curves, 4, 4)  # a frame outside the trial
