@@ -313,6 +313,7 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
 {
   static_assert(REBASE == 64 && NRAY * NBW <= 2048, "segment fields: 11-bit slot, 6-bit offsets");
   __shared__ float4 s_rec[3][NRAY];      // per ray: X, Y, Z, dX, dY, dZ as double-floats
+  __shared__ float s_trim[6][NRAY];      // per ray: the walk's RayTrim (1 / dC, C / dC per axis)
   __shared__ float2 s_part[NRAY * NBW];  // per segment slot: block start, then (sum, compensation)
   __shared__ unsigned s_seg[NRAY * NBW]; // per segment slot: slot | js << 11 | je << 17
   __shared__ unsigned s_ord[NRAY * NBW]; // the segments, longest first
@@ -353,6 +354,11 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
       s_rec[0][tid] = make_float4(rs.X.h, rs.X.l, rs.Y.h, rs.Y.l);
       s_rec[1][tid] = make_float4(rs.Z.h, rs.Z.l, rs.dX.h, rs.dX.l);
       s_rec[2][tid] = make_float4(rs.dY.h, rs.dY.l, rs.dZ.h, rs.dZ.l);
+      const RayTrim rt = ray_trim(rs);
+      for (int i = 0; i < 3; ++i) {
+        s_trim[i][tid] = rt.ia[i];
+        s_trim[3 + i][tid] = rt.ca[i];
+      }
       done = false;
     }
     CellWalk cw = cell_walk(B.vol, rs, 0);
@@ -365,7 +371,7 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
       // ---- walk: up to NBW segments of this ray
       int n = 0;
       if (!done)
-        done = walk_segments(cw, occ, ws, [&](int kb, int js, int je) {
+        done = walk_segments(cw, occ, &s_trim[0][tid], NRAY, ws, [&](int kb, int js, int je) {
           if (n == NBW) return false;
           const int slot = tid * NBW + n++;
           s_seg[slot] = (unsigned)slot | (unsigned)js << 11 | (unsigned)je << 17;
@@ -1258,7 +1264,7 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
       B.scale[v] = bones[i].step[v] * vh->dev.norm / bones[i].intensity[v];
       B.cutoff_raw[v] = bones[i].cutoff[v] / vh->dev.norm;
       uint8_t* occ = nullptr;
-      if (e->alloc(occ, occupancy_cells(vh->dev))) {
+      if (e->alloc(occ, occ_grid_bytes(occupancy_cells(vh->dev)))) {
         delete e;
         return ASC_ERR_NOMEM;
       }

@@ -390,24 +390,24 @@ __global__ void __launch_bounds__(RB) k_hdist_sad(const float* __restrict__ f, c
   }
 }
 
-// Occupancy of OCC^3-voxel cells (OCC, OCC_LO, OCC_HI, OCC_PAD in
-// asc_march.cuh), margin cells included: one thread per cell takes the
-// maximum over the cell and its apron (voxels outside the volume are 0).
+// Occupancy bytes and boxes of OCC^3-voxel cells (occ_cell in asc_march.cuh),
+// margin cells included: one thread per cell scans the cell and its apron
+// (voxels outside the volume are 0).
 template <int STORE>
 __global__ void k_occupancy(DevVolume V, float cutoff_raw, uint8_t* __restrict__ occ)
 {
   const int px = occ_dim(V.nx), py = occ_dim(V.ny), pz = occ_dim(V.nz);
+  const int n = px * py * pz;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= px * py * pz) return;
+  if (c >= n) return;
   const int cx = c % px - OCC_PAD, cy = (c / px) % py - OCC_PAD, cz = c / (px * py) - OCC_PAD;
-  float mx = -1.0f;
-  const int lo = -OCC_LO, hi = OCC + OCC_HI;
-  for (int z = max(cz * OCC + lo, 0); z < min(cz * OCC + hi, V.nz); ++z)
-    for (int y = max(cy * OCC + lo, 0); y < min(cy * OCC + hi, V.ny); ++y)
-      for (int x = max(cx * OCC + lo, 0); x < min(cx * OCC + hi, V.nx); ++x) {
-        mx = fmaxf(mx, voxel_value<STORE>(V, (size_t)(z + PAD) * V.pxy + (size_t)(y + PAD) * V.px + (x + PAD)));
-      }
-  occ[c] = mx > cutoff_raw ? 1 : 0;
+  int box[4];
+  occ[c] = occ_cell(cx, cy, cz, V.nx, V.ny, V.nz, cutoff_raw,
+                    [&](int x, int y, int z) {
+                      return voxel_value<STORE>(V, (size_t)(z + PAD) * V.pxy + (size_t)(y + PAD) * V.px + (x + PAD));
+                    },
+                    box);
+  reinterpret_cast<int4*>(occ + occ_box_offset((size_t)n))[c] = make_int4(box[0], box[1], box[2], box[3]);
 }
 
 int g_empty_skip = 1;
@@ -832,7 +832,7 @@ ASC_API int asc_raycast(asc_volume vol, const double imv[16], const float vp[4],
     const float cut = cutoff / v->dev.norm;
     if (!v->occ) {
       Gate g(device_gate());
-      ASC_CUDA(cudaMalloc(&v->occ, occupancy_cells(v->dev)));
+      ASC_CUDA(cudaMalloc(&v->occ, occ_grid_bytes(occupancy_cells(v->dev))));
     }
     if (!(v->occ_cutoff == cut)) {
       build_occupancy(v->dev, cut, v->occ, S(stream));

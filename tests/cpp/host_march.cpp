@@ -39,20 +39,21 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
   const float cut = cutoff / V.norm;
   // occupancy as k_occupancy builds it
   const int bx = occ_dim(nx), by = occ_dim(ny), bz = occ_dim(nz);
-  std::vector<uint8_t> occ((size_t)bx * by * bz);
+  const size_t ncell = (size_t)bx * by * bz;
+  std::vector<uint8_t> occ(occ_grid_bytes(ncell) + 16);
+  uint8_t* o8 = occ.data() + ((16 - ((uintptr_t)occ.data() & 15)) & 15);  // 16-byte aligned, as cudaMalloc's
   for (int cz = -OCC_PAD; cz < bz - OCC_PAD; ++cz)
     for (int cy = -OCC_PAD; cy < by - OCC_PAD; ++cy)
       for (int cx = -OCC_PAD; cx < bx - OCC_PAD; ++cx) {
-        float mx = -1.0f;
-        for (int z = std::max(cz * OCC - OCC_LO, 0); z < std::min(cz * OCC + OCC + OCC_HI, nz); ++z)
-          for (int y = std::max(cy * OCC - OCC_LO, 0); y < std::min(cy * OCC + OCC + OCC_HI, ny); ++y)
-            for (int x = std::max(cx * OCC - OCC_LO, 0); x < std::min(cx * OCC + OCC + OCC_HI, nx); ++x) {
-              const size_t i = (size_t)(z + PAD) * pxy + (size_t)(y + PAD) * px + (x + PAD);
-              mx = std::max(mx, storage == ASC_STORE_BF16 ? voxel_value<ASC_STORE_BF16>(V, i)
-                                : storage == ASC_STORE_F32 ? voxel_value<ASC_STORE_F32>(V, i)
-                                                           : voxel_value<ASC_STORE_U16>(V, i));
-            }
-        occ[((size_t)(cz + OCC_PAD) * by + (cy + OCC_PAD)) * bx + (cx + OCC_PAD)] = mx > cut ? 1 : 0;
+        const size_t c = ((size_t)(cz + OCC_PAD) * by + (cy + OCC_PAD)) * bx + (cx + OCC_PAD);
+        int box[4];
+        o8[c] = occ_cell(cx, cy, cz, nx, ny, nz, cut, [&](int x, int y, int z) {
+          const size_t i = (size_t)(z + PAD) * pxy + (size_t)(y + PAD) * px + (x + PAD);
+          return storage == ASC_STORE_BF16  ? voxel_value<ASC_STORE_BF16>(V, i)
+                 : storage == ASC_STORE_F32 ? voxel_value<ASC_STORE_F32>(V, i)
+                                            : voxel_value<ASC_STORE_U16>(V, i);
+        }, box);
+        std::memcpy(o8 + occ_box_offset(ncell) + 16 * c, box, 16);
       }
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
@@ -63,7 +64,7 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
       df_split((double)vp[2] / (double)w, sx.h, sx.l);
       df_split((double)vp[3] / (double)h, sy.h, sy.l);
       if (ray_setup(m, vp, x, y, sx, sy, step, nx, ny, nz, r)) {
-        const uint8_t* o = skip ? occ.data() : nullptr;
+        const uint8_t* o = skip ? o8 : nullptr;
         const float acc = storage == ASC_STORE_BF16  ? march<ASC_STORE_BF16>(V, o, r, cut)
                           : storage == ASC_STORE_F32 ? march<ASC_STORE_F32>(V, o, r, cut)
                                                      : march<ASC_STORE_U16>(V, o, r, cut);

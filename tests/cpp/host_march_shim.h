@@ -36,11 +36,13 @@ inline unsigned __byte_perm(unsigned x, unsigned y, unsigned s)
   return r;
 }
 inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
+inline float __int_as_float(int u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline int __float2int_rd(float f) { return (int)std::floor(f); }
 template <class T> inline T __ldg(const T* p) { return *p; }
 struct float2 { float x, y; };
 struct uint2 { unsigned x, y; };
 struct float4 { float x, y, z, w; };
+struct int4 { int x, y, z, w; };
 inline float2 make_float2(float x, float y) { return {x, y}; }
 struct __half2_raw { unsigned short x, y; };
 struct __half2 { unsigned short x, y; };
