@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
       s_rec[0][tid] = make_float4(rs.X.h, rs.X.l, rs.Y.h, rs.Y.l);
       s_rec[1][tid] = make_float4(rs.Z.h, rs.Z.l, rs.dX.h, rs.dX.l);
       s_rec[2][tid] = make_float4(rs.dY.h, rs.dY.l, rs.dZ.h, rs.dZ.l);
-      const RayTrim rt = ray_trim(rs);
+      const RayTrim rt = ray_trim(B.vol, rs);
       for (int i = 0; i < 3; ++i) {
         s_trim[i][tid] = rt.ia[i];
         s_trim[3 + i][tid] = rt.ca[i];

@@ -189,22 +189,25 @@ __device__ __forceinline__ float lerp_tap(const Taps<STORE>& t, int k, float a)
 // cutoff and adds exactly nothing to the DRR (RayCaster_kernels.cu:189); the
 // march skips it.
 //
-// An occupied cell also keeps the box of its voxels above the cutoff, grown
-// by two voxels per side: a sample can touch such a voxel v only at texel
-// coordinates in [v-1, v+1) per axis, and the second voxel of margin covers
-// the walk's placement error.  The walk marches only the cell's samples that
-// lie in the box, so a cell occupied by a few voxels costs a few samples.
+// An occupied cell also keeps the box of its voxels above the cutoff: a
+// sample can touch such a voxel v only at texel coordinates in [v-1, v+1)
+// per axis, and an eighth of a voxel of margin covers the walk's placement
+// error (FP32 positions, ~1e-4 voxel).  The walk marches only the cell's
+// samples that lie in the box, so a cell occupied by a few voxels costs a few
+// samples.  Bounds are int16 eighths of a voxel, so trimming applies to
+// volumes of at most OCC_TRIM_MAX voxels per axis.
 constexpr int OCC = 8;
 constexpr int OCC_LO = 1, OCC_HI = 2;  // apron voxels below and above a cell
 // The grid holds OCC_PAD cells of margin on every side (cells -2 .. b + 1 of
 // an axis of b cells), so that a walk, whose cells stay within one of the
 // box's, indexes it without clamping.
 constexpr int OCC_PAD = 2;
+constexpr int OCC_TRIM_MAX = 4094;
 __host__ __device__ __forceinline__ int occ_dim(int n) { return (n + OCC - 1) / OCC + 2 * OCC_PAD; }
 
 // The grid of n cells: n occupancy bytes, then at the next 16-byte boundary
 // n boxes, each an int4 of (lo | hi << 16) per axis x, y, z (int16 texel
-// coordinates) and a spare word.
+// coordinates in eighths of a voxel) and a spare word.
 __host__ __device__ __forceinline__ size_t occ_box_offset(size_t n) { return (n + 15) & ~(size_t)15; }
 __host__ __device__ __forceinline__ size_t occ_grid_bytes(size_t n) { return occ_box_offset(n) + 16 * n; }
 
@@ -222,12 +225,12 @@ __host__ __device__ inline uint8_t occ_cell(int cx, int cy, int cz, int nx, int 
       for (int x = max(cx * OCC + a, 0); x < min(cx * OCC + e, nx); ++x)
         if (val(x, y, z) > cutoff) {
           any = true;
-          lo[0] = min(lo[0], x - 2);
-          hi[0] = max(hi[0], x + 2);
-          lo[1] = min(lo[1], y - 2);
-          hi[1] = max(hi[1], y + 2);
-          lo[2] = min(lo[2], z - 2);
-          hi[2] = max(hi[2], z + 2);
+          lo[0] = min(lo[0], 8 * (x - 1) - 1);
+          hi[0] = max(hi[0], 8 * (x + 1) + 1);
+          lo[1] = min(lo[1], 8 * (y - 1) - 1);
+          hi[1] = max(hi[1], 8 * (y + 1) + 1);
+          lo[2] = min(lo[2], 8 * (z - 1) - 1);
+          hi[2] = max(hi[2], 8 * (z + 1) + 1);
         }
   for (int i = 0; i < 3; ++i) box[i] = (lo[i] & 0xffff) | (int)((unsigned)hi[i] << 16);
   box[3] = 0;
@@ -460,20 +463,23 @@ __device__ __forceinline__ CellWalk cell_walk(const DevVolume& V, const RaySetup
 }
 
 // The walk's view of one ray for trimming a cell to its box: per axis
-// 1 / dC and C / dC (sample k sits at C - k dC), NaN for an axis the ray runs
-// parallel to (no bound from it).
+// 1 / (8 dC) and C / dC (sample k sits at C - k dC; box bounds are eighths
+// of a voxel), NaN for an axis the ray runs parallel to and for every axis
+// of a volume too large for the boxes (no bound from it).
 struct RayTrim {
   float ia[3], ca[3];
 };
 
-__device__ __forceinline__ RayTrim ray_trim(const RaySetup& r)
+__device__ __forceinline__ RayTrim ray_trim(const DevVolume& V, const RaySetup& r)
 {
   RayTrim t;
   const float C[3] = {r.X.h, r.Y.h, r.Z.h}, d[3] = {r.dX.h, r.dY.h, r.dZ.h};
+  const bool big = V.nx > OCC_TRIM_MAX || V.ny > OCC_TRIM_MAX || V.nz > OCC_TRIM_MAX;
   for (int i = 0; i < 3; ++i) {
-    const bool par = d[i] == 0.f;
-    t.ia[i] = par ? 0.f : __frcp_rn(d[i]);
-    t.ca[i] = par ? __int_as_float(0x7fffffff) : C[i] * t.ia[i];
+    const bool none = big || d[i] == 0.f;
+    const float ia = none ? 0.f : __frcp_rn(d[i]);
+    t.ia[i] = 0.125f * ia;
+    t.ca[i] = none ? __int_as_float(0x7fffffff) : C[i] * ia;
   }
   return t;
 }
@@ -673,7 +679,7 @@ __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __rest
   if (r.K <= 0) return 0.f;
   CellWalk w = cell_walk(V, r, 0);
   WalkState s{0, r.K - 1, 0, -1, 0};
-  const RayTrim t = ray_trim(r);
+  const RayTrim t = ray_trim(V, r);
   const float tf[6] = {t.ia[0], t.ia[1], t.ia[2], t.ca[0], t.ca[1], t.ca[2]};
   df total{0.f, 0.f};
   walk_segments(w, occ, tf, 1, s, [&](int kb, int js, int je) {
