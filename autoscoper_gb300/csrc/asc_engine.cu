@@ -335,7 +335,9 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
     const int k = s_k;
     const IV& r = b.iv[k];
     const int t = tile - b.roff[k];
-    const int x = (t % r.rtx) * RTX + (tid % RTX), y = (t / r.rtx) * RTY + (tid / RTX);
+    // each warp takes an 8 x 4 block of the 16 x 16 tile (coherent walks)
+    const int x = (t % r.rtx) * RTX + (tid & 7) + 8 * ((tid >> 5) & 1),
+              y = (t / r.rtx) * RTY + ((tid >> 3) & 3) + 4 * (tid >> 6);
     const bool valid = x < r.w && y < r.h;
     const BoneDev& B = sc->bones[r.bone];
     const int v = k % nv;
