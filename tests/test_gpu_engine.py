@@ -179,3 +179,26 @@ def test_pso_converges():
     for b in range(2):
         assert cost2[b] < tr.minimization_func(b, np.zeros(6))
         _check(cost2[b], tr.minimization_func(b, best2[b]))
+
+
+def test_hidden_bone_scores_the_empty_mask(scene):
+    """RayCaster::setVisible(false) renders zeros (RayCaster.cpp:131-134): a
+    hidden bone's views score the empty-mask cost (1 - 1e5 for NCC) batched
+    and plain, its images export a zero DRR and mask, and showing it again
+    restores the costs."""
+    sc, tr = scene
+    eng = api.Engine(sc, max_items=8)
+    bones = np.array([0, 1], np.int32)
+    man = np.zeros((2, 6))
+    before, _ = eng.eval(bones, man)
+    eng.set_visible(0, False)
+    cost, vcost = eng.eval(bones, man)
+    pcost, pvcost = eng.eval(bones, man, plain=True)
+    assert np.all(vcost[0] == 1.0 - 1e5) and np.all(pvcost[0] == 1.0 - 1e5)
+    assert cost[0] == 9999.0 and pcost[0] == 9999.0  # a negative total is the reference's 9999
+    assert cost[1] == before[1]
+    rad, drr, mask = eng.image_data(0, 0, np.asarray(sc.poses[0], np.float64))
+    assert not drr.any() and not mask.any()
+    eng.set_visible(0, True)
+    again, _ = eng.eval(bones, man)
+    assert np.array_equal(again, before)
