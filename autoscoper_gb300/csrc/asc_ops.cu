@@ -720,6 +720,10 @@ ASC_API int asc_volume_create(const void* data, int W, int H, int D, int bps, co
     vmin = a; vmax = b;
   }
   if (mn[0] > mx[0] || mn[1] > mx[1] || mn[2] > mx[2]) return ASC_ERR_EMPTY;
+  // the march indexes the padded grid in 32-bit arithmetic
+  if ((double)(mx[0] - mn[0] + 1 + 2 * PAD) * (mx[1] - mn[1] + 1 + 2 * PAD) * (mx[2] - mn[2] + 1 + 2 * PAD) >=
+      2147483648.0)
+    return ASC_ERR_RANGE;
   auto* v = new asc_volume_host();
   v->occ = nullptr;
   v->occ_cutoff = NAN;

@@ -90,7 +90,8 @@ int asc_mem_info(size_t *free_bytes, size_t *total_bytes);
  * (libautoscoper/src/VolumeDescription.cpp:152-305): flips, crops to the
  * non-zero box, records min/max and the normalisation constants, uploads.
  * data: width*height*depth voxels (x fastest), bps 8 or 16; scale: voxel
- * size in mm; flip: 0/1 per axis; storage: ASC_STORE_*. */
+ * size in mm; flip: 0/1 per axis; storage: ASC_STORE_*.  A cropped volume of
+ * 2^31 voxels or more (its two-voxel padding included) is ASC_ERR_RANGE. */
 int asc_volume_create(const void *data, int width, int height, int depth, int bps, const double scale[3],
                       const int flip[3], int storage, asc_volume *out);
 /* invScale(), invTrans(), transCenter(), minValue(), maxValue() and the
