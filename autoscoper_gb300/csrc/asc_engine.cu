@@ -819,7 +819,7 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
       // tile: f = DRR * mask over fdrr, g = rad * mask over the chain result,
       // the m > 0.5 flags in the free blur buffer
       const unsigned n = (unsigned)r.w * (unsigned)r.h;
-      const bool tree = sc->coverage == ASC_SUM_TREE;
+      const bool tree = sc->coverage == ASC_SUM_TREE && tree_needed(n);  // else every pixel counts
       const bool sad = sc->cf_model != 0;
       float* gres = bufs[rres];
       float* flag = bufs[2];

@@ -126,6 +126,18 @@ __device__ __forceinline__ bool image_coords_r(const float* ip, const float* vp,
   return !(s < 0.0f || t < 0.0f || s > 1.0f || t > 1.0f);
 }
 
+// Whether the reference's multi-level sum() of n elements drops any: only a
+// level whose thread count is not a power of two does (tree_keep).
+__host__ __device__ __forceinline__ bool tree_needed(unsigned n)
+{
+  while (n > 1) {
+    unsigned T = n < 256u ? n : 256u;
+    if (T & (T - 1)) return true;
+    n = (n + T - 1) / T;
+  }
+  return false;
+}
+
 // Whether element i of n reaches the reference's multi-level sum()
 // (Ncc_kernels.cu:151-187): levels of T = min(n_l, 256) threads fold shared
 // memory with s = T/2, T/4, ..., never reading slots at or above 2s.

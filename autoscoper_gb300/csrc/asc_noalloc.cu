@@ -26,7 +26,6 @@ struct ReduceScratch {
 __global__ void __launch_bounds__(256) k_ncc(const float* __restrict__ f, const float* __restrict__ g,
                                              const float* __restrict__ mask, unsigned n, int tree, ReduceScratch sc,
                                              double* __restrict__ result);
-bool tree_needed(unsigned n);
 
 }  // namespace asc
 

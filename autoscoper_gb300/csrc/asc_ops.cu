@@ -427,16 +427,6 @@ void build_occupancy(const DevVolume& V, float cutoff_raw, uint8_t* occ, cudaStr
 
 // ---------------------------------------------------------------- host side
 
-bool tree_needed(unsigned n)
-{
-  while (n > 1) {
-    unsigned T = n < 256u ? n : 256u;
-    if (T & (T - 1)) return true;
-    n = (n + T - 1) / T;
-  }
-  return false;
-}
-
 int launch_filter(const asc_filter_desc& f, const float* in, float* out, int w, int h, cudaStream_t s)
 {
   if (w <= 0 || h <= 0) return ASC_OK;
