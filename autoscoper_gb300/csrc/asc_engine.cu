@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
 // single ray.  A ray with more than NBW segments takes further passes.
 template <int STORE>
 __device__ __forceinline__ void march_segments(const DevVolume& V, const float4 (*rec)[NRAY], const unsigned* ord,
-                                               float2* part, int nseg, int* grab, float cut,
+                                               float* part, int nseg, int* grab, float cut,
                                                unsigned long long& marched, unsigned long long& slots)
 {
   const unsigned FULL = 0xffffffffu;
@@ -299,7 +299,7 @@ __device__ __forceinline__ void march_segments(const DevVolume& V, const float4 
       r.dX = df{q1.z, q1.w};
       r.dY = df{q2.x, q2.y};
       r.dZ = df{q2.z, q2.w};
-      const int kb = __float_as_int(part[slot].x);  // the block start, until the sum replaces it
+      const int kb = __float_as_int(part[slot]);  // the block start, until the sum replaces it
       part[slot] = march_block<STORE>(V, r, kb, js, je, cut);
       len = je - js + 1;
     }
@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
   static_assert(REBASE == 64 && NRAY * NBW <= 2048, "segment fields: 11-bit slot, 6-bit offsets");
   __shared__ float4 s_rec[3][NRAY];      // per ray: X, Y, Z, dX, dY, dZ as double-floats
   __shared__ float s_trim[6][NRAY];      // per ray: the walk's RayTrim (1 / dC, C / dC per axis)
-  __shared__ float2 s_part[NRAY * NBW];  // per segment slot: block start, then (sum, compensation)
+  __shared__ float s_part[NRAY * NBW];   // per segment slot: the block start (int bits), then its sum
   __shared__ unsigned s_seg[NRAY * NBW]; // per segment slot: slot | js << 11 | je << 17
   __shared__ unsigned s_ord[NRAY * NBW]; // the segments, longest first
   __shared__ int s_cnt[REBASE];          // segments per length - 1, then placement cursors
@@ -377,7 +377,7 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
           if (n == NBW) return false;
           const int slot = tid * NBW + n++;
           s_seg[slot] = (unsigned)slot | (unsigned)js << 11 | (unsigned)je << 17;
-          s_part[slot].x = __int_as_float(kb);
+          s_part[slot] = __int_as_float(kb);
           atomicAdd(&s_cnt[je - js], 1);
           return true;
         });

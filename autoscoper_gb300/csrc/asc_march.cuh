@@ -587,11 +587,13 @@ __device__ __forceinline__ void coord_base(df C, df dC, float k, int& base_i, fl
 
 // Samples kb + js .. kb + je of one march block (kb a multiple of REBASE) of
 // cuda_volume_render_kernel's loop (RayCaster_kernels.cu:187-195; t = far -
-// k).  Returns the block's compensated (Kahan) sum of raw samples above
-// cutoff_raw as (sum, compensation); a sample at or below the cutoff leaves
-// both untouched, so trimming samples that add nothing changes no bit.
+// k).  Returns the block's FP32 sum of raw samples above cutoff_raw (at most
+// REBASE of them, so its relative error stays below ~4e-6 and typically near
+// 1e-7; the blocks are combined in double-float); a sample at or below the
+// cutoff leaves it untouched, so trimming samples that add nothing changes no
+// bit.
 template <int STORE>
-__device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup& r, int kb, int js, int je,
+__device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup& r, int kb, int js, int je,
                                               float cutoff_raw)
 {
   const uint32_t* __restrict__ P = V.pairs;
@@ -616,7 +618,7 @@ __device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup
                           ((unsigned)(bix + PAD) - BM);
   const unsigned imax = ASC_QUADS ? (unsigned)(V.nz + 2 * PAD - 1) * pxy - 1u
                                   : (unsigned)(V.nz + 2 * PAD - 1) * pxy - px - 1u;
-  float acc = 0.f, comp = 0.f;
+  float acc = 0.f;
   float j = (float)js;
   // the taps' voxel index and weights of sample j (j * the low part of d
   // stays below 1e-6 voxel for j < REBASE)
@@ -637,12 +639,7 @@ __device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup
     const float f0 = fmaf(wy, e10 - e00, e00);
     const float f1 = fmaf(wy, e11 - e01, e01);
     const float v = fmaf(wz, f1 - f0, f0);
-    if (v > cutoff_raw) {
-      const float y = v - comp;
-      const float tt = acc + y;
-      comp = (tt - acc) - y;
-      acc = tt;
-    }
+    if (v > cutoff_raw) acc += v;
   };
   // Two samples per iteration over two tap sets A and B, each sample's loads
   // issued one sample ahead of its arithmetic (after the last sample they
@@ -658,14 +655,14 @@ __device__ __forceinline__ float2 march_block(const DevVolume& V, const RaySetup
     accumulate(B, bx, by, bz);
   }
   if (k == je) accumulate(A, ax, ay, az);
-  return make_float2(acc, comp);
+  return acc;
 }
 
-// Adds a block's compensated sum (value sum - compensation) to the ray's
-// double-float total; blocks that added nothing leave it untouched.
-__device__ __forceinline__ void add_block(df& total, float2 p)
+// Adds a block's sum to the ray's double-float total; blocks that added
+// nothing leave it untouched.
+__device__ __forceinline__ void add_block(df& total, float p)
 {
-  if (p.x != 0.f || p.y != 0.f) total = df_add(df_add(total, df{p.x, 0.f}), df{-p.y, 0.f});
+  if (p != 0.f) total = df_add(total, df{p, 0.f});
 }
 
 // One whole ray: the march blocks that hold occupied samples, in order, each
