@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
 {
   static_assert(REBASE == 64 && NRAY * NBW <= 2048, "segment fields: 11-bit slot, 6-bit offsets");
   __shared__ float4 s_rec[3][NRAY];      // per ray: X, Y, Z, dX, dY, dZ as double-floats
-  __shared__ float s_trim[6][NRAY];      // per ray: the walk's RayTrim (1 / dC, C / dC per axis)
+  __shared__ float s_trim[3][NRAY];      // per ray: RayTrim's 1 / (8 dC) per axis (its C is in s_rec)
   __shared__ float s_part[NRAY * NBW];   // per segment slot: the block start (int bits), then its sum
   __shared__ unsigned s_seg[NRAY * NBW]; // per segment slot: slot | js << 11 | je << 17
   __shared__ unsigned s_ord[NRAY * NBW]; // the segments, longest first
@@ -357,10 +357,7 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
       s_rec[1][tid] = make_float4(rs.Z.h, rs.Z.l, rs.dX.h, rs.dX.l);
       s_rec[2][tid] = make_float4(rs.dY.h, rs.dY.l, rs.dZ.h, rs.dZ.l);
       const RayTrim rt = ray_trim(B.vol, rs);
-      for (int i = 0; i < 3; ++i) {
-        s_trim[i][tid] = rt.ia[i];
-        s_trim[3 + i][tid] = rt.ca[i];
-      }
+      for (int i = 0; i < 3; ++i) s_trim[i][tid] = rt.ia[i];
       done = false;
     }
     CellWalk cw = cell_walk(B.vol, rs, 0);
@@ -372,8 +369,12 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
       __syncthreads();
       // ---- walk: up to NBW segments of this ray
       int n = 0;
+      const auto trim = [&](int i, float& ia, float& c) {
+        ia = s_trim[i][tid];
+        c = i == 0 ? s_rec[0][tid].x : (i == 1 ? s_rec[0][tid].z : s_rec[1][tid].x);  // X.h, Y.h, Z.h
+      };
       if (!done)
-        done = walk_segments(cw, occ, &s_trim[0][tid], NRAY, ws, [&](int kb, int js, int je) {
+        done = walk_segments(cw, occ, trim, ws, [&](int kb, int js, int je) {
           if (n == NBW) return false;
           const int slot = tid * NBW + n++;
           s_seg[slot] = (unsigned)slot | (unsigned)js << 11 | (unsigned)je << 17;

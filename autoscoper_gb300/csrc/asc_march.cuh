@@ -463,11 +463,11 @@ __device__ __forceinline__ CellWalk cell_walk(const DevVolume& V, const RaySetup
 }
 
 // The walk's view of one ray for trimming a cell to its box: per axis
-// 1 / (8 dC) and C / dC (sample k sits at C - k dC; box bounds are eighths
-// of a voxel), NaN for an axis the ray runs parallel to and for every axis
-// of a volume too large for the boxes (no bound from it).
+// ia = 1 / (8 dC) (box bounds are eighths of a voxel) and the start C
+// (sample k sits at C - k dC); ia is NaN for an axis the ray runs parallel
+// to and for every axis of a volume too large for the boxes (no bound).
 struct RayTrim {
-  float ia[3], ca[3];
+  float ia[3], c[3];
 };
 
 __device__ __forceinline__ RayTrim ray_trim(const DevVolume& V, const RaySetup& r)
@@ -476,10 +476,8 @@ __device__ __forceinline__ RayTrim ray_trim(const DevVolume& V, const RaySetup& 
   const float C[3] = {r.X.h, r.Y.h, r.Z.h}, d[3] = {r.dX.h, r.dY.h, r.dZ.h};
   const bool big = V.nx > OCC_TRIM_MAX || V.ny > OCC_TRIM_MAX || V.nz > OCC_TRIM_MAX;
   for (int i = 0; i < 3; ++i) {
-    const bool none = big || d[i] == 0.f;
-    const float ia = none ? 0.f : __frcp_rn(d[i]);
-    t.ia[i] = 0.125f * ia;
-    t.ca[i] = none ? __int_as_float(0x7fffffff) : C[i] * ia;
+    t.ia[i] = big || d[i] == 0.f ? __int_as_float(0x7fffffff) : 0.125f * __frcp_rn(d[i]);
+    t.c[i] = C[i];
   }
   return t;
 }
@@ -499,9 +497,9 @@ struct WalkState {
 // where it stopped.  Returns true when the ray is done.  Without `occ` every
 // sample counts as occupied.  The steps are bounded by the cells the ray
 // crosses; past that bound the rest of the ray counts as occupied.
-template <class Emit>
-__device__ __forceinline__ bool walk_segments(CellWalk& w, const uint8_t* __restrict__ occ, const float* trim,
-                                              int tstride, WalkState& s, Emit&& emit)
+template <class Emit, class Trim>
+__device__ __forceinline__ bool walk_segments(CellWalk& w, const uint8_t* __restrict__ occ, Trim&& trim, WalkState& s,
+                                              Emit&& emit)
 {
   const int4* __restrict__ boxes = occ ? (const int4*)(occ + occ_box_offset((size_t)w.last + 1)) : nullptr;
   int steps = w.steps;
@@ -521,14 +519,16 @@ __device__ __forceinline__ bool walk_segments(CellWalk& w, const uint8_t* __rest
       // add the cell's samples [a, ke] that lie in its box to the open block(s)
       int ke = tn < kendf ? (int)floorf(tn) : s.kend;
       int a = (int)floorf(tp) + 1;
-      if (looked && trim) {
+      if (looked) {
         const int4 bx = __ldg(boxes + min((unsigned)w.cell, w.last));
         float klo = -1.0e9f, khi = 1.0e9f;
         const int pk[3] = {bx.x, bx.y, bx.z};
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
           const float lo = (float)((pk[i] << 16) >> 16), hi = (float)(pk[i] >> 16);
-          const float ia = trim[i * tstride], ca = trim[(3 + i) * tstride];
+          float ia, c;
+          trim(i, ia, c);  // the ray's RayTrim entries of axis i
+          const float ca = 8.0f * c * ia;  // C / dC
           const float k1 = fmaf(-hi, ia, ca), k2 = fmaf(-lo, ia, ca);
           klo = fmaxf(klo, fminf(k1, k2));  // a NaN bound (parallel axis) leaves klo and khi
           khi = fminf(khi, fmaxf(k1, k2));
@@ -677,9 +677,11 @@ __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __rest
   CellWalk w = cell_walk(V, r, 0);
   WalkState s{0, r.K - 1, 0, -1, 0};
   const RayTrim t = ray_trim(V, r);
-  const float tf[6] = {t.ia[0], t.ia[1], t.ia[2], t.ca[0], t.ca[1], t.ca[2]};
   df total{0.f, 0.f};
-  walk_segments(w, occ, tf, 1, s, [&](int kb, int js, int je) {
+  walk_segments(w, occ, [&](int i, float& ia, float& c) {
+    ia = t.ia[i];
+    c = t.c[i];
+  }, s, [&](int kb, int js, int je) {
     add_block(total, march_block<STORE>(V, r, kb, js, je, cutoff_raw));
     return true;
   });
