@@ -352,15 +352,19 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
       if (lane == 0) atomicAdd(&b.C->samples, (unsigned long long)tot);
     }
     bool done = true;
+    CellWalk cw = cell_walk(B.vol, rs, 0);
     if (hit && rs.K > 0) {
       s_rec[0][tid] = make_float4(rs.X.h, rs.X.l, rs.Y.h, rs.Y.l);
       s_rec[1][tid] = make_float4(rs.Z.h, rs.Z.l, rs.dX.h, rs.dX.l);
       s_rec[2][tid] = make_float4(rs.dY.h, rs.dY.l, rs.dZ.h, rs.dZ.l);
-      const RayTrim rt = ray_trim(B.vol, rs);
-      for (int i = 0; i < 3; ++i) s_trim[i][tid] = rt.ia[i];
+      // ray_trim's 1 / (8 dC) from the walk's crossing intervals (dt = 8 / |dC|)
+      const bool big = B.vol.nx > OCC_TRIM_MAX || B.vol.ny > OCC_TRIM_MAX || B.vol.nz > OCC_TRIM_MAX;
+      const float nan = __int_as_float(0x7fffffff);
+      s_trim[0][tid] = big || cw.ix == 0 ? nan : (cw.ix < 0 ? cw.dtx : -cw.dtx) * (1.0f / 64.0f);
+      s_trim[1][tid] = big || cw.iy == 0 ? nan : (cw.iy < 0 ? cw.dty : -cw.dty) * (1.0f / 64.0f);
+      s_trim[2][tid] = big || cw.iz == 0 ? nan : (cw.iz < 0 ? cw.dtz : -cw.dtz) * (1.0f / 64.0f);
       done = false;
     }
-    CellWalk cw = cell_walk(B.vol, rs, 0);
     WalkState ws{0, rs.K - 1, 0, -1, 0};
     df total{0.f, 0.f};
     for (;;) {
