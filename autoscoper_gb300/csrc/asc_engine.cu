@@ -2,10 +2,10 @@
 // for many (bone, manipulator) candidates per pass, with the scene resident
 // on the device.
 //
-// One evaluation is four launches on one stream:
-//   k_setup       1 block:  FP64 pose composition, view matrices, viewports
-//                            (Tracker.cpp:603-634) and the tile layout of every
-//                            (item, view) crop, with prefix sums;
+// One evaluation is four launches on one stream (five with cf_model 1):
+//   k_setup_iv    a thread per (item, view): FP64 pose composition, view
+//                            matrix, viewport (Tracker.cpp:603-634) and crop;
+//   k_setup       1 block:  the tile layout of every crop, with prefix sums;
 //   k_ray         persistent: 16x16-ray tiles pulled from an atomic queue,
 //                            DRRs written to a packed buffer;
 //   k_view        persistent: 48x48 output tiles pulled from a queue; each
@@ -88,6 +88,7 @@ struct IV {
   float sx[2], sy[2];  // vp[2] / w and vp[3] / h as double-floats
   int w, h, ok, bone;
   int rtx, rty, ftx, fty;
+  int err;        // the crop exceeded the render size (the reference throws)
   long long pix;  // offset of this crop in the DRR buffer
 };
 
@@ -134,9 +135,85 @@ __device__ void finish_item(const SceneDev* sc, const Bufs& b, int item, double*
 }
 
 // ---------------------------------------------------------------- k_setup
-__global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc, int n_items,
-                                                 const int* __restrict__ bone_in, const double* __restrict__ manip,
-                                                 Bufs b, double* __restrict__ cost, double* __restrict__ view_cost_out)
+// One (item, view) of trackFrame's set-up: the pose (minimizationFunc), the
+// folded matrix, the viewport and crop size, its ray and view tile counts.
+__device__ void setup_iv(const SceneDev* __restrict__ sc, int k, const int* __restrict__ bone_in,
+                         const double* __restrict__ manip, const Bufs& b)
+{
+  const int nv = sc->n_views;
+  const int item = k / nv, v = k % nv;
+  IV r;
+  memset(&r, 0, sizeof r);
+  int bi = bone_in[item];
+  if (bi < 0 || bi >= sc->n_bones) bi = 0;
+  r.bone = bi;
+  const BoneDev& B = sc->bones[bi];
+  const ViewDev& V = sc->views[v];
+  // minimizationFunc: pose . V^-1 . manip . V, then the xyzypr round trip
+  double base[12], man[12], t1[12], t2[12], xyz[6];
+  frame_from_xyzypr(B.base, base);
+  frame_from_axis_angle(manip + 6 * item, man);
+  frame_mul(base, B.pivot_inv, t1);
+  frame_mul(t1, man, t2);
+  frame_mul(t2, B.pivot, t1);
+  frame_to_xyzypr(t1, xyz);
+  frame_from_xyzypr(xyz, t1);
+  // trackFrame (1a)-(1c)
+  double mv[12], imv[12], imv16[16], vp[4];
+  frame_mul(V.cam_inv, t1, mv);
+  frame_inverse(mv, imv);
+  frame_row_matrix(imv, imv16);
+  fold_matrix(imv16, B.inv_scale, B.inv_trans, r.m);
+  double vc = 0.0;
+  if (!calculate_viewport(mv, V.cam, V.ip, B.inv_scale, B.inv_trans, vp)) {
+    vc = 9999.0;  // Tracker.cpp:614-617
+  } else {
+    double fw = vp[2] * sc->rw / V.cvp[2], fh = vp[3] * sc->rh / V.cvp[3];
+    unsigned w = fw > 0 ? (unsigned)fw : 0u, h = fh > 0 ? (unsigned)fh : 0u;
+    if (w > (unsigned)sc->rw || h > (unsigned)sc->rh) {
+      r.err = 1;  // the reference throws (Tracker.cpp:625-629)
+      w = 0;
+      h = 0;
+    }
+    r.w = (int)w;
+    r.h = (int)h;
+    for (int j = 0; j < 4; ++j) r.vp[j] = (float)vp[j];
+    if (w > 0 && h > 0) {
+      df_split((double)r.vp[2] / (double)w, r.sx[0], r.sx[1]);
+      df_split((double)r.vp[3] / (double)h, r.sy[0], r.sy[1]);
+    }
+    if (w == 0 || h == 0 || !B.visible) {
+      // an empty crop, or the all-zero DRR of a hidden volume (RayCaster.cpp:131-134),
+      // whose mask is empty: the degenerate NCC (1e5), or the SAD of no pixels
+      vc = sc->cf_model ? 0.0 : 1.0 - 1e5;
+    } else {
+      r.ok = 1;
+      r.rtx = (r.w + RTX - 1) / RTX;
+      r.rty = (r.h + RTY - 1) / RTY;
+      r.ftx = (r.w + VT - 1) / VT;
+      r.fty = (r.h + VT - 1) / VT;
+    }
+  }
+  b.iv[k] = r;
+  b.vcost[k] = vc;
+  b.ivt[k] = 0;
+}
+
+// Every (item, view) at once: the FP64 set-up of each runs on its own thread
+// across the GPU.
+__global__ void __launch_bounds__(128) k_setup_iv(const SceneDev* __restrict__ sc, int n_items,
+                                                  const int* __restrict__ bone_in, const double* __restrict__ manip,
+                                                  Bufs b)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n_items * sc->n_views) setup_iv(sc, k, bone_in, manip, b);
+}
+
+// The layout of a batch after k_setup_iv: prefix sums of the tile counts and
+// crop sizes (ray tiles, view tiles, DRR offsets), the batch counters, and
+// the items' view tickets (views finished in set-up count as arrived).
+__global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc, int n_items, Bufs b,
+                                                 double* __restrict__ cost)
 {
   __shared__ int s_err;
   const int nv = sc->n_views, n_iv = n_items * nv;
@@ -147,66 +224,11 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
   int rsum = 0, fsum = 0;
   long long psum = 0;
   for (int k = i0; k < i1; ++k) {
-    const int item = k / nv, v = k % nv;
-    IV r;
-    memset(&r, 0, sizeof r);
-    int bi = bone_in[item];
-    if (bi < 0 || bi >= sc->n_bones) bi = 0;
-    r.bone = bi;
-    const BoneDev& B = sc->bones[bi];
-    const ViewDev& V = sc->views[v];
-    // minimizationFunc: pose . V^-1 . manip . V, then the xyzypr round trip
-    double base[12], man[12], t1[12], t2[12], xyz[6];
-    frame_from_xyzypr(B.base, base);
-    frame_from_axis_angle(manip + 6 * item, man);
-    frame_mul(base, B.pivot_inv, t1);
-    frame_mul(t1, man, t2);
-    frame_mul(t2, B.pivot, t1);
-    frame_to_xyzypr(t1, xyz);
-    frame_from_xyzypr(xyz, t1);
-    // trackFrame (1a)-(1c)
-    double mv[12], imv[12], imv16[16], vp[4];
-    frame_mul(V.cam_inv, t1, mv);
-    frame_inverse(mv, imv);
-    frame_row_matrix(imv, imv16);
-    fold_matrix(imv16, B.inv_scale, B.inv_trans, r.m);
-    double vc = 0.0;
-    if (!calculate_viewport(mv, V.cam, V.ip, B.inv_scale, B.inv_trans, vp)) {
-      vc = 9999.0;  // Tracker.cpp:614-617
-    } else {
-      double fw = vp[2] * sc->rw / V.cvp[2], fh = vp[3] * sc->rh / V.cvp[3];
-      unsigned w = fw > 0 ? (unsigned)fw : 0u, h = fh > 0 ? (unsigned)fh : 0u;
-      if (w > (unsigned)sc->rw || h > (unsigned)sc->rh) {
-        s_err = ASC_ERR_RANGE;  // the reference throws (Tracker.cpp:625-629)
-        w = 0;
-        h = 0;
-      }
-      r.w = (int)w;
-      r.h = (int)h;
-      for (int j = 0; j < 4; ++j) r.vp[j] = (float)vp[j];
-      if (w > 0 && h > 0) {
-        df_split((double)r.vp[2] / (double)w, r.sx[0], r.sx[1]);
-        df_split((double)r.vp[3] / (double)h, r.sy[0], r.sy[1]);
-      }
-      if (w == 0 || h == 0 || !B.visible) {
-        // an empty crop, or the all-zero DRR of a hidden volume (RayCaster.cpp:131-134),
-        // whose mask is empty: the degenerate NCC (1e5), or the SAD of no pixels
-        vc = sc->cf_model ? 0.0 : 1.0 - 1e5;
-      } else {
-        r.ok = 1;
-        r.rtx = (r.w + RTX - 1) / RTX;
-        r.rty = (r.h + RTY - 1) / RTY;
-        r.ftx = (r.w + VT - 1) / VT;
-        r.fty = (r.h + VT - 1) / VT;
-      }
-    }
-    r.pix = psum;  // local offset, fixed up after the scan
+    const IV& r = b.iv[k];
+    if (r.err) s_err = ASC_ERR_RANGE;
     psum += (long long)r.w * r.h;
     rsum += r.rtx * r.rty;
     fsum += r.ftx * r.fty;
-    b.iv[k] = r;
-    b.vcost[k] = vc;
-    b.ivt[k] = 0;
   }
   // block-wide exclusive scan of (rsum, fsum, psum)
   __shared__ long long sp[1024];
@@ -229,9 +251,10 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
   long long pbase = sp[threadIdx.x] - psum;
   for (int k = i0; k < i1; ++k) {
     IV& r = b.iv[k];
-    r.pix += pbase;
+    r.pix = pbase;
     b.roff[k] = rbase;
     b.foff[k] = fbase;
+    pbase += (long long)r.w * r.h;
     rbase += r.rtx * r.rty;
     fbase += r.ftx * r.fty;
   }
@@ -258,7 +281,6 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
     b.itt[item] = pre;
     if (pre == (unsigned)nv) finish_item(sc, b, item, cost);
   }
-  (void)view_cost_out;
 }
 
 // ---------------------------------------------------------------- k_ray
@@ -1387,7 +1409,8 @@ static int engine_launch(asc_engine e, int n, const int* bone, const double* man
 {
   const bool prof = e->prof && !capturing;
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[0], s));
-  k_setup<<<1, 1024, 0, s>>>(e->dev, n, bone, manip, e->b, cost, vcost);
+  k_setup_iv<<<(n * e->n_views + 127) / 128, 128, 0, s>>>(e->dev, n, bone, manip, e->b);
+  k_setup<<<1, 1024, 0, s>>>(e->dev, n, e->b, cost);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[1], s));
   k_ray<<<e->sms * ASC_RAY_MINBLOCKS, NRAY, 0, s>>>(e->dev, e->b, g_empty_skip);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[2], s));

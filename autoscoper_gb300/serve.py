@@ -21,6 +21,7 @@ from __future__ import annotations
 import ctypes as C
 import threading
 import time
+import zlib
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional
 
@@ -249,7 +250,7 @@ def make_job(job_id, rng, subject, arrival, vol_range=(64, 320), view_range=(256
              frames=(1, 50), particles=(32, 128), iterations=20, render_targets=None):
     """A seeded synthetic job of the mixed serving workload.  The subject id
     fixes the volumes (same subject = same phantoms)."""
-    srng = np.random.default_rng(abs(hash(subject)) % (2 ** 32))
+    srng = np.random.default_rng(zlib.crc32(subject.encode()))  # stable across processes (str hash is salted)
     nb = int(srng.integers(bones[0], bones[1] + 1))
     shapes = []
     for _ in range(nb):
