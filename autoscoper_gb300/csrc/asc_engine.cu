@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
   const unsigned FULL = 0xffffffffu;
   const int tid = threadIdx.x, lane = tid & 31;
   const int nv = sc->n_views;
-  unsigned long long marched = 0, slots = 0;
+  unsigned long long marched = 0, slots = 0, sampled = 0;
   for (;;) {
     if (tid == 0) {
       const int tl = atomicAdd(&b.C->rnext, 1);
@@ -368,11 +368,9 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
     RaySetup rs{};
     const bool hit = valid && ray_setup(r.m, r.vp, x, y, df{r.sx[0], r.sx[1]}, df{r.sy[0], r.sy[1]}, B.step[v],
                                         B.vol.nx, B.vol.ny, B.vol.nz, rs);
-    {
-      // trilinear samples of the reference's march (the work figure of the roofline)
-      const unsigned tot = __reduce_add_sync(FULL, hit ? (unsigned)rs.K : 0u);
-      if (lane == 0) atomicAdd(&b.C->samples, (unsigned long long)tot);
-    }
+    // trilinear samples of the reference's march (the work figure of the
+    // roofline), counted per warp and added to the global count once at the end
+    sampled += __reduce_add_sync(FULL, hit ? (unsigned)rs.K : 0u);
     bool done = true;
     CellWalk cw = cell_walk(B.vol, rs, 0);
     if (hit && rs.K > 0) {
@@ -446,6 +444,7 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
     }
     if (valid) b.drr[r.pix + (long long)y * r.w + x] = fminf(fmaxf((total.h + total.l) * B.scale[v], 0.f), 1.f);
   }
+  if (lane == 0 && sampled) atomicAdd(&b.C->samples, sampled);
   if (lane == 0 && slots) {
     atomicAdd(&b.C->marched, marched);
     atomicAdd(&b.C->slots, slots);
