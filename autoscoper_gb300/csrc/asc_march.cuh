@@ -179,6 +179,47 @@ __device__ __forceinline__ float lerp_tap(const Taps<STORE>& t, int k, float a)
     return lerp_pair<STORE>(t.w[k], a);
 }
 
+// ---- two samples at once.  The packed FP32 operations of sm_100 and later
+// (fma.rn.f32x2, add.f32x2) apply one IEEE operation to each half, so every
+// value below equals, bit for bit, the scalar expression cited beside it.
+__device__ __forceinline__ float2 bcast2(float a) { return make_float2(a, a); }
+// a - b with one rounding
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, bcast2(-1.0f), a); }
+
+// lerp_tap of tap word k of samples A (x) and B (y), weights a
+template <int STORE>
+__device__ __forceinline__ float2 lerp_tap2(const Taps<STORE>& A, const Taps<STORE>& B, int k, float2 a)
+{
+  float2 lo, hi;
+  if constexpr (STORE == ASC_STORE_F32) {
+    lo = make_float2(A.p[k].x, B.p[k].x);
+    hi = make_float2(A.p[k].y, B.p[k].y);
+  } else if constexpr (STORE == ASC_STORE_U16) {
+    // lerp_pair: fmaf(a, hi - lo, lo - 2^23) of the biased halves
+    lo = make_float2(__uint_as_float(__byte_perm(A.w[k], 0x4b000000u, 0x7610)),
+                     __uint_as_float(__byte_perm(B.w[k], 0x4b000000u, 0x7610)));
+    hi = make_float2(__uint_as_float(__byte_perm(A.w[k], 0x4b000000u, 0x7632)),
+                     __uint_as_float(__byte_perm(B.w[k], 0x4b000000u, 0x7632)));
+    return __ffma2_rn(a, sub2(hi, lo), __fadd2_rn(lo, bcast2(-8388608.0f)));
+  } else {
+    unpack<STORE>(A.w[k], lo.x, hi.x);
+    unpack<STORE>(B.w[k], lo.y, hi.y);
+  }
+  return __ffma2_rn(a, sub2(hi, lo), lo);  // fmaf(a, hi - lo, lo)
+}
+
+// The trilinear values of samples A and B (march_block's accumulate)
+template <int STORE>
+__device__ __forceinline__ float2 trilinear2(const Taps<STORE>& A, const Taps<STORE>& B, float2 wx, float2 wy,
+                                             float2 wz)
+{
+  const float2 e00 = lerp_tap2<STORE>(A, B, 0, wx), e10 = lerp_tap2<STORE>(A, B, 1, wx);
+  const float2 e01 = lerp_tap2<STORE>(A, B, 2, wx), e11 = lerp_tap2<STORE>(A, B, 3, wx);
+  const float2 f0 = __ffma2_rn(wy, sub2(e10, e00), e00);  // fmaf(wy, e10 - e00, e00)
+  const float2 f1 = __ffma2_rn(wy, sub2(e11, e01), e01);
+  return __ffma2_rn(wz, sub2(f1, f0), f0);                // fmaf(wz, f1 - f0, f0)
+}
+
 // Occupancy of OCC^3-voxel cells for one cutoff (OCC = 8): cell (cx, cy, cz)
 // is empty (byte 0) when every voxel of [8c-1, 8c+10) on each axis is <=
 // cutoff.  That range holds the taps of nonzero weight of every sample at a
@@ -641,20 +682,36 @@ __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup&
     const float v = fmaf(wz, f1 - f0, f0);
     if (v > cutoff_raw) acc += v;
   };
-  // Two samples per iteration over two tap sets A and B, each sample's loads
-  // issued one sample ahead of its arithmetic (after the last sample they
-  // re-read clamped, in-bounds words); the samples add in order.
-  float ax, ay, az, bx, by, bz;
-  Taps<STORE> A = fetch_taps<STORE>(P, locate(j, ax, ay, az), px, pxy);
+  // Samples two at a time (jj and jj + 1) in packed pairs, both samples'
+  // loads issued together; the samples add in order.
+  const float2 dX2 = bcast2(-dXh), dY2 = bcast2(-dYh), dZ2 = bcast2(-dZh);
+  const float2 fx2 = bcast2(fx), fy2 = bcast2(fy), fz2 = bcast2(fz);
+  auto locate2 = [&](float jj, float2& wx, float2& wy, float2& wz, unsigned& ia, unsigned& ib) {
+    const float2 J = make_float2(jj, jj + 1.0f);
+    const float2 X = __ffma2_rn(J, dX2, fx2), Y = __ffma2_rn(J, dY2, fy2), Z = __ffma2_rn(J, dZ2, fz2);
+    const float2 tx = __fadd2_rd(X, bcast2(M)), ty = __fadd2_rd(Y, bcast2(M)), tz = __fadd2_rd(Z, bcast2(M));
+    wx = sub2(X, __fadd2_rn(tx, bcast2(-M)));
+    wy = sub2(Y, __fadd2_rn(ty, bcast2(-M)));
+    wz = sub2(Z, __fadd2_rn(tz, bcast2(-M)));
+    ia = min(__float_as_uint(tz.x) * pxy + __float_as_uint(ty.x) * px + __float_as_uint(tx.x) + i_base, imax);
+    ib = min(__float_as_uint(tz.y) * pxy + __float_as_uint(ty.y) * px + __float_as_uint(tx.y) + i_base, imax);
+  };
   int k = js;
   for (; k < je; k += 2) {
-    const Taps<STORE> B = fetch_taps<STORE>(P, locate(j + 1.0f, bx, by, bz), px, pxy);
-    accumulate(A, ax, ay, az);
+    float2 wx, wy, wz;
+    unsigned ia, ib;
+    locate2(j, wx, wy, wz, ia, ib);
+    const Taps<STORE> A = fetch_taps<STORE>(P, ia, px, pxy), B = fetch_taps<STORE>(P, ib, px, pxy);
+    const float2 v = trilinear2<STORE>(A, B, wx, wy, wz);
+    if (v.x > cutoff_raw) acc += v.x;
+    if (v.y > cutoff_raw) acc += v.y;
     j += 2.0f;
-    A = fetch_taps<STORE>(P, locate(j, ax, ay, az), px, pxy);
-    accumulate(B, bx, by, bz);
   }
-  if (k == je) accumulate(A, ax, ay, az);
+  if (k == je) {
+    float ax, ay, az;
+    const Taps<STORE> A = fetch_taps<STORE>(P, locate(j, ax, ay, az), px, pxy);
+    accumulate(A, ax, ay, az);
+  }
   return acc;
 }
 

@@ -40,6 +40,10 @@ inline float __int_as_float(int u) { float f; std::memcpy(&f, &u, 4); return f; 
 inline int __float2int_rd(float f) { return (int)std::floor(f); }
 template <class T> inline T __ldg(const T* p) { return *p; }
 struct float2 { float x, y; };
+// the packed FP32 pairs of sm_100: one IEEE operation per half
+inline float2 __ffma2_rn(float2 a, float2 b, float2 c) { return {std::fma(a.x, b.x, c.x), std::fma(a.y, b.y, c.y)}; }
+inline float2 __fadd2_rn(float2 a, float2 b) { return {__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y)}; }
+inline float2 __fadd2_rd(float2 a, float2 b) { return {__fadd_rd(a.x, b.x), __fadd_rd(a.y, b.y)}; }
 struct uint2 { unsigned x, y; };
 struct float4 { float x, y, z, w; };
 struct int4 { int x, y, z, w; };
