@@ -275,7 +275,12 @@ __host__ __device__ inline uint8_t occ_cell(int cx, int cy, int cz, int nx, int 
         }
   for (int i = 0; i < 3; ++i) box[i] = (lo[i] & 0xffff) | (int)((unsigned)hi[i] << 16);
   box[3] = 0;
-  return any ? 1 : 0;
+  // byte 2: the box covers the cell with a voxel to spare on every side, so
+  // trimming keeps every sample the walk places in the cell
+  const int c[3] = {cx, cy, cz};
+  bool covers = true;
+  for (int i = 0; i < 3; ++i) covers = covers && lo[i] <= 8 * (OCC * c[i] - 1) && hi[i] >= 8 * (OCC * c[i] + OCC + 1);
+  return any ? (covers ? 2 : 1) : 0;
 }
 
 
@@ -548,19 +553,20 @@ __device__ __forceinline__ bool walk_segments(CellWalk& w, const uint8_t* __rest
   const float kendf = (float)s.kend;
   float tp = (float)s.k - 0.5f;
   while (tp < kendf) {
-    bool full = true, looked = false;
+    bool full = true;
+    unsigned cb = 0;  // the cell's occupancy byte; 1: trim to the box
     float tn = 3.0e38f;
     if (occ && steps > 0) {
       tn = fminf(w.tx, fminf(w.ty, w.tz));
-      full = __ldg(occ + min((unsigned)w.cell, w.last)) != 0;
-      looked = true;
+      cb = __ldg(occ + min((unsigned)w.cell, w.last));
+      full = cb != 0;
       --steps;
     }
     if (full) {
       // add the cell's samples [a, ke] that lie in its box to the open block(s)
       int ke = tn < kendf ? (int)floorf(tn) : s.kend;
       int a = (int)floorf(tp) + 1;
-      if (looked) {
+      if (cb == 1) {
         const int4 bx = __ldg(boxes + min((unsigned)w.cell, w.last));
         float klo = -1.0e9f, khi = 1.0e9f;
         const int pk[3] = {bx.x, bx.y, bx.z};
