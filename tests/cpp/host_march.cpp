@@ -76,3 +76,22 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
     }
   return 0;
 }
+
+// Occupancy bytes of a u16 volume's padded grid at a cutoff (normalized as
+// hm_raycast's): counts[b] = cells with byte b (0 empty, 1 trimmed to the
+// box, 2 box covering the cell).
+extern "C" void hm_occupancy(const uint16_t* vol, int nx, int ny, int nz, float cutoff, long long* counts)
+{
+  const float cut = cutoff / (1.0f / 65535.0f);
+  const int bx = occ_dim(nx), by = occ_dim(ny), bz = occ_dim(nz);
+  counts[0] = counts[1] = counts[2] = 0;
+  for (int cz = -OCC_PAD; cz < bz - OCC_PAD; ++cz)
+    for (int cy = -OCC_PAD; cy < by - OCC_PAD; ++cy)
+      for (int cx = -OCC_PAD; cx < bx - OCC_PAD; ++cx) {
+        int box[4];
+        const uint8_t b = occ_cell(cx, cy, cz, nx, ny, nz, cut, [&](int x, int y, int z) {
+          return (float)vol[((size_t)z * ny + y) * nx + x];
+        }, box);
+        ++counts[b];
+      }
+}

@@ -23,6 +23,7 @@ def hm(tmp_path_factory):
     lib = C.CDLL(so)
     lib.hm_raycast.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    lib.hm_occupancy.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_void_p]
     return lib
 
 
@@ -61,6 +62,13 @@ def test_host_march_matches_oracle(hm, small):
 
 def test_host_march_skip_is_exact(hm, small):
     sc, tr = small
+    # the grid holds all three kinds of cell: empty, trimmed to its box, and
+    # covered by its box (whose trim the walk skips)
+    vd = tr.vd[0]
+    vol = np.ascontiguousarray(vd.data, np.uint16)
+    counts = np.zeros(3, np.int64)
+    hm.hm_occupancy(vol.ctypes.data, vd.dims[0], vd.dims[1], vd.dims[2], sc.ray[0][0].cutoff, counts.ctypes.data)
+    assert counts.min() > 0, counts
     rng = np.random.default_rng(2)
     for _ in range(3):
         pose = S.perturb(sc.truth[0], rng, 3.0, 30.0).astype(np.float64)
