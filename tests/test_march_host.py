@@ -81,6 +81,26 @@ def test_host_march_skip_is_exact(hm, small):
                 assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("angles", [(0.0, 0.0, 0.0), (90.0, 0.0, 0.0), (0.0, 90.0, 90.0)])
+def test_host_march_skip_is_exact_axis_aligned(hm, small, angles):
+    """Rays along the grid axes: coordinates that stay on a cell plane or a
+    voxel centre, and axes with no bound (NaN trim)."""
+    sc, tr = small
+    pose = np.array(sc.truth[0], np.float64)
+    pose[3:] = angles
+    for vi in range(2):
+        ok, m, vp, w, h = tr.view_setup(0, vi, pose)
+        if not ok:
+            continue
+        rp = sc.ray[vi][0]
+        a, ns = run(hm, tr.vd[0], m, vp, rp, w, h, skip=1)
+        b, _ = run(hm, tr.vd[0], m, vp, rp, w, h, skip=0)
+        assert ns.sum() > 0 and np.array_equal(a, b)
+        ref = O.raycast(tr.vd[0], m, np.float32(vp).astype(np.float64), float(np.float32(rp.step)),
+                        float(np.float32(rp.intensity)), float(np.float32(rp.cutoff)), w, h)
+        assert np.abs(a - ref).max() < 1e-6
+
+
 def test_host_march_bf16_matches_oracle_on_rounded_volume(hm, small):
     sc, tr = small
     vd = tr.vd[0]
