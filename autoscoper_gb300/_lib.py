@@ -59,6 +59,7 @@ SIGNATURES = {
     "asc_free": (i32, [vp]),
     "asc_memcpy_h2d": (i32, [vp, vp, C.c_size_t, vp]),
     "asc_memcpy_d2h": (i32, [vp, vp, C.c_size_t, vp]),
+    "asc_memcpy_d2d": (i32, [vp, vp, C.c_size_t, vp]),
     "asc_memset": (i32, [vp, i32, C.c_size_t, vp]),
     "asc_stream_sync": (i32, [vp]),
     "asc_device_sync": (i32, []),
@@ -72,6 +73,7 @@ SIGNATURES = {
     "asc_host_alloc": (i32, [P(vp), C.c_size_t]),
     "asc_host_free": (i32, [vp]),
     "asc_mem_info": (i32, [P(C.c_size_t), P(C.c_size_t)]),
+    "asc_probe_read_bandwidth": (i32, [C.c_size_t, i32, P(f64), P(f32)]),
     "asc_volume_create": (i32, [vp, i32, i32, i32, i32, P(f64), P(i32), i32, P(vp)]),
     "asc_volume_info": (i32, [vp, P(f32), P(f32), P(f64), P(f32), P(f32), P(i32)]),
     "asc_volume_destroy": (i32, [vp]),

@@ -506,6 +506,17 @@ __device__ __forceinline__ float contrast_pow(float axy, float v, float e1, floa
 // stay inside the block's shared memory (VR rows of slack follow the
 // buffers) and their results are discarded.
 constexpr int VR = 4;
+
+// k_view's dynamic shared memory, in 4-byte words: three E x E stage
+// buffers, the VT x VT tile, VR + 2 rows of slack for the column units'
+// reads past a band, then the region's per-column and per-row radiograph
+// mapping (texel index and weight each).
+__host__ __device__ constexpr size_t view_tail_floats(int E)
+{
+  return (size_t)3 * E * E + (size_t)VT * VT + (size_t)(VR + 2) * E;
+}
+__host__ __device__ constexpr size_t view_smem_floats(int E) { return view_tail_floats(E) + (size_t)4 * E; }
+constexpr int kNoTexel = -0x7fffffff;  // a column or row that maps outside the radiograph
 template <class F>
 __device__ __forceinline__ void for_units(int y0, int y1, int x0, int x1, F&& f)
 {
@@ -739,43 +750,25 @@ __device__ int run_chain(const FilterDev* fl, int nf, int H, float* bufs[3], flo
   return cur;
 }
 
-__device__ __forceinline__ float wsum(float v)
-{
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-template <int N>
-__device__ void bsum(float (&v)[N], float* red)
-{
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-  for (int k = 0; k < N; ++k) v[k] = wsum(v[k]);
-  if (lane == 0)
-#pragma unroll
-    for (int k = 0; k < N; ++k) red[warp * N + k] = v[k];
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < N; ++k) {
-    float s = 0.f;
-    for (int j = 0; j < nw; ++j) s += red[j * N + k];
-    v[k] = s;
-  }
-  __syncthreads();
-}
-
 __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
     k_view(const SceneDev* __restrict__ sc, Bufs b, double* __restrict__ cost, double* __restrict__ view_cost_out)
 {
   extern __shared__ float smem[];
   __shared__ int s_tile, s_k;
   __shared__ bool s_last;
-  __shared__ float red[8 * 6];
+  __shared__ float red[8 * 6 * 2];
+  __shared__ double ds[6], dc[3];
   __shared__ float wsh[32];
   const int E = sc->E, eh = (E - VT) / 2;
   float* bufs[3] = {smem, smem + E * E, smem + 2 * E * E};
   float* fdrr = smem + 3 * E * E;        // VT x VT final DRR, then f = DRR * mask
   Moments* msh = (Moments*)smem;          // reused by the merge
+  // per region column / row: the radiograph texel pair and weight of the
+  // film-plane mapping (image_axis; kNoTexel where the pixel maps outside)
+  int* tcx = (int*)(smem + view_tail_floats(E));
+  float* tax = (float*)(tcx + E);
+  int* tcy = (int*)(tax + E);
+  float* tay = (float*)(tcy + E);
   const int nv = sc->n_views;
   for (;;) {
     if (threadIdx.x == 0) {
@@ -795,9 +788,6 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
     const int rx0 = tx0 - eh, ry0 = ty0 - eh;
     const Region g{rx0, ry0, E, r.w, r.h, rx0 >= 0 && ry0 >= 0 && rx0 + E <= r.w && ry0 + E <= r.h};
     const float* drr = b.drr + r.pix;
-    // reciprocals for the film-plane mapping of this crop's pixels
-    const float fw = (float)r.w, fh = (float)r.h;
-    const float rcp[4] = {__frcp_rn(fw), __frcp_rn(fh), __frcp_rn(V.ipf[2]), __frcp_rn(V.ipf[3])};
     // ---- DRR region; a region of zeros filters to zeros (every filter maps
     // 0 to 0), so its tile masks out entirely and adds nothing to the moments
     bool live;
@@ -819,9 +809,20 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
       for_band(lo, hi, lo, hi, [&](int ry, int rx) { nz |= bufs[0][ry * E + rx] != 0.f; });
       live = __syncthreads_or(nz);
     }
-    float s[6] = {0, 0, 0, 0, 0, 0}, c[3] = {0, 0, 0};
-    float cnt = 0.f, mf = 0.f, mg = 0.f;
+    float mf = 0.f, mg = 0.f;
     if (live) {
+      // the film-plane mapping of the region's columns and rows, in FP64
+      // (visible to the radiograph band after the chain's barriers)
+      for (int i = threadIdx.x; i < 2 * E; i += VNT) {
+        const bool row = i >= E;
+        const int j = row ? i - E : i;
+        int k;
+        float a = 0.f;
+        const bool ok = row ? image_axis(r.vp[1], r.vp[3], g.y0 + j, r.h, V.ipf[1], V.ipf[3], V.rad_h, true, k, a)
+                            : image_axis(r.vp[0], r.vp[2], g.x0 + j, r.w, V.ipf[0], V.ipf[2], V.rad_w, false, k, a);
+        (row ? tcy : tcx)[j] = ok ? k : kNoTexel;
+        (row ? tay : tax)[j] = a;
+      }
       // ---- DRR chain
       {
         int res = run_chain(V.fdrr, V.n_drr, V.h_drr, bufs, wsh, g, eh);
@@ -833,9 +834,10 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
       {
         const int lo = eh - V.h_rad, hi = eh + VT + V.h_rad;
         for_band(lo, hi, lo, hi, [&](int ry, int rx) {
-          float val = 0.f, s, tt;
-          if ((g.in || inside(g, ry, rx)) && image_coords_r(V.ipf, r.vp, g.x0 + rx, g.y0 + ry, fw, fh, rcp, s, tt))
-            val = 1.0f - bilinear(V.rad, V.rad_bps, V.rad_w, V.rad_h, s, tt);
+          float val = 0.f;
+          const int kx = tcx[rx], ky = tcy[ry];
+          if ((g.in || inside(g, ry, rx)) && kx != kNoTexel && ky != kNoTexel)
+            val = 1.0f - bilinear_at(V.rad, V.rad_bps, V.rad_w, V.rad_h, kx, tax[rx], ky, tay[ry]);
           bufs[0][ry * E + rx] = val;
         });
         __syncthreads();
@@ -849,6 +851,12 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
       const bool sad = sc->cf_model != 0;
       float* gres = bufs[rres];
       float* flag = bufs[2];
+      // per tile: the pixels with mask 1 and their sums of f and g.  The
+      // mask is 0 or 1 and f, g are 0 where it is 0, so these are also the
+      // covered pixels' sums of mask, f and g.  Plain FP32 suffices for them:
+      // an error in a tile's mean moves the centred moments only at second
+      // order; the products are the sums that need compensating.
+      float s[3] = {0.f, 0.f, 0.f};
       for (int i = threadIdx.x; i < VT * VT; i += VNT) {
         const int ly = i / VT, lx = i % VT, x = tx0 + lx, y = ty0 + ly;
         const int gi = (eh + ly) * E + eh + lx;
@@ -857,22 +865,21 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
           float d = fdrr[i], gg = gres[gi];
           float bg = 1.0f;
           if (V.bg && V.bg_thr >= 0.f) {
-            float ss, tt;
-            bg = image_coords_r(V.ipf, r.vp, x, y, fw, fh, rcp, ss, tt)
-                   ? (V.bg_thr <= bilinear(V.bg, 32, V.bg_w, V.bg_h, ss, tt) ? 1.0f : 0.0f)
+            int kx, ky;
+            float ax, ay;
+            bg = image_axis(r.vp[0], r.vp[2], x, r.w, V.ipf[0], V.ipf[2], V.bg_w, false, kx, ax) &&
+                     image_axis(r.vp[1], r.vp[3], y, r.h, V.ipf[1], V.ipf[3], V.bg_h, true, ky, ay)
+                   ? (V.bg_thr <= bilinear_at(V.bg, 32, V.bg_w, V.bg_h, kx, ax, ky, ay) ? 1.0f : 0.0f)
                    : 0.0f;
           }
           float m = bg * (d != 0.0f ? 1.0f : 0.0f);
           f = d * m;
           gm = gg * m;
-          s[0] += m;
-          s[1] += f;
-          s[2] += gm;
           if (m > 0.5f) {
             fl = 1.f;
-            s[3] += 1.f;
-            s[4] += f;
-            s[5] += gm;
+            s[0] += 1.f;
+            s[1] += f;
+            s[2] += gm;
           }
         }
         fdrr[i] = f;
@@ -881,22 +888,27 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
         // SAD needs the view's global means first: keep f and g for k_sad
         if (sad && x < r.w && y < r.h) b.fg[r.pix + (long long)y * r.w + x] = make_float2(f, gm);
       }
-      bsum<6>(s, red);
-      cnt = s[3];
-      mf = cnt > 0 ? s[4] / cnt : 0.f;
-      mg = cnt > 0 ? s[5] / cnt : 0.f;
+      block_sum_f<3>(s, red, ds + 3);
+      if (threadIdx.x < 3) ds[threadIdx.x] = ds[3 + threadIdx.x];  // read by thread 0 after the next barrier
+      const double cnt = ds[3];
+      mf = cnt > 0 ? (float)(ds[4] / cnt) : 0.f;
+      mg = cnt > 0 ? (float)(ds[5] / cnt) : 0.f;
+      DFs c[3] = {};  // compensated co-moments about (mf, mg)
       for (int i = threadIdx.x; i < VT * VT && !sad; i += VNT)
         if (flag[i] != 0.f) {
           const int ly = i / VT, lx = i % VT;
           float a = fdrr[i] - mf, bb = gres[(eh + ly) * E + eh + lx] - mg;
-          c[0] = fmaf(a, a, c[0]);
-          c[1] = fmaf(bb, bb, c[1]);
-          c[2] = fmaf(a, bb, c[2]);
+          dfs_add_prod(c[0], a, a);
+          dfs_add_prod(c[1], bb, bb);
+          dfs_add_prod(c[2], a, bb);
         }
-      bsum<3>(c, red);
-    }  // live
+      block_sum_dfs<3>(c, red, dc);
+    } else if (threadIdx.x == 0) {  // a tile of zeros adds nothing
+      for (int j = 0; j < 6; ++j) ds[j] = 0.0;
+      for (int j = 0; j < 3; ++j) dc[j] = 0.0;
+    }
     if (threadIdx.x == 0) {
-      Moments p = {s[0], s[1], s[2], cnt, mf, mg, c[0], c[1], c[2]};
+      Moments p = tile_moments(ds, dc, mf, mg);
       b.part[tile] = p;
       __threadfence();
       s_last = atomicAdd(&b.ivt[k], 1u) == (unsigned)(r.ftx * r.fty) - 1;
@@ -1269,7 +1281,7 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
   S.E = VT + 2 * hmax;
   // three E x E stage buffers and the final tile must fit one block's shared
   // memory (227 KB less the static arrays)
-  if ((3 * S.E * S.E + VT * VT + (VR + 2) * S.E) * sizeof(float) > 224 * 1024) {
+  if (view_smem_floats(S.E) * sizeof(float) > 224 * 1024) {
     delete e;
     return ASC_ERR_RANGE;
   }
@@ -1344,7 +1356,7 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
   }
   // three stage buffers, the final DRR tile and VR + 2 rows of slack for the
   // column units' reads past a band
-  e->smem = (size_t)(3 * S.E * S.E + VT * VT + (VR + 2) * S.E) * sizeof(float);
+  e->smem = view_smem_floats(S.E) * sizeof(float);
   e->smem = std::max(e->smem, (size_t)256 * sizeof(Moments));
   int dev = 0;
   cudaGetDevice(&dev);

@@ -76,54 +76,46 @@ __device__ __forceinline__ float image_texel(const void* img, int bps, int i)
   return __ldg((const float*)img + i);
 }
 
-__device__ __forceinline__ float bilinear(const void* img, int bps, int W, int H, float s, float t)
+// One axis of the film-plane mapping of RadRenderer / BackgroundRenderer
+// (RadRenderer_kernels.cu:103-112, BackgroundRenderer_kernels.cu:103-116) and
+// of tex2D's linear filter set-up, in FP64: pixel x of a crop n pixels wide
+// over the viewport span [v0, v0 + vw) lands at the normalized coordinate
+// s = (u - i0) / iw + 0.5 (columns) or s = 0.5 - (u - i0) / iw (rows, `rows`)
+// of an image N texels wide; false when s leaves [0, 1] (the pixel is 0).
+// Otherwise k receives the lower texel of the bilinear pair (floor(s N - 0.5),
+// held to [-1, N] before the edge clamp) and a the weight of the upper one.
+// In FP32 the coordinate s N - 0.5 of a 1024-texel image carries errors of
+// ~1e-4 texel, which on a noisy radiograph moves the sample by ~5e-6; the
+// FP64 mapping leaves only the FP32 interpolation's rounding.  Every pixel
+// of a column (row) shares its column's (row's) mapping, so a tile computes
+// it once per column and once per row.
+__host__ __device__ __forceinline__ bool image_axis(double v0, double vw, int x, int n, double i0, double iw, int N,
+                                                    bool rows, int& k, float& a)
 {
-  float X = s * W - 0.5f, Y = t * H - 0.5f;
-  float fx = floorf(X), fy = floorf(Y);
-  float ax = X - fx, ay = Y - fy;
-  fx = fminf(fmaxf(fx, -1.0f), (float)W);
-  fy = fminf(fmaxf(fy, -1.0f), (float)H);
-  int x0 = (int)fx, y0 = (int)fy;
+  const double u = v0 + vw * ((double)x / (double)n);
+  const double q = (u - i0) / iw;
+  const double s = rows ? 0.5 - q : q + 0.5;
+  if (s < 0.0 || s > 1.0) return false;
+  const double X = s * N - 0.5;
+  double fl = floor(X);
+  a = (float)(X - fl);
+  fl = fmin(fmax(fl, -1.0), (double)N);
+  k = (int)fl;
+  return true;
+}
+
+// Bilinear read of an 8/16-bit (normalized) or float image at the pair
+// (x0, x0 + 1) x (y0, y0 + 1) with weights (ax, ay), clamp-to-edge, as
+// tex2D<float> with the reference's texture object (cutil_create_tex_obj.h:6-28).
+__device__ __forceinline__ float bilinear_at(const void* img, int bps, int W, int H, int x0, float ax, int y0,
+                                             float ay)
+{
   int xa = min(max(x0, 0), W - 1), xb = min(max(x0 + 1, 0), W - 1);
   int ya = min(max(y0, 0), H - 1), yb = min(max(y0 + 1, 0), H - 1);
   float v00 = image_texel(img, bps, ya * W + xa), v01 = image_texel(img, bps, ya * W + xb);
   float v10 = image_texel(img, bps, yb * W + xa), v11 = image_texel(img, bps, yb * W + xb);
   float r0 = fmaf(ax, v01 - v00, v00), r1 = fmaf(ax, v11 - v10, v10);
   return fmaf(ay, r1 - r0, r0);
-}
-
-// Film-plane pixel of RadRenderer/BackgroundRenderer (RadRenderer_kernels.cu:103-107).
-__device__ __forceinline__ bool image_coords(const float* ip, const float* vp, int x, int y, int w, int h, float& s,
-                                             float& t)
-{
-  float u = vp[0] + vp[2] * (x / (float)w);
-  float v = vp[1] + vp[3] * (y / (float)h);
-  s = (u - ip[0]) / ip[2] + 0.5f;
-  t = 0.5f - (v - ip[1]) / ip[3];
-  return !(s < 0.0f || t < 0.0f || s > 1.0f || t > 1.0f);
-}
-
-// a / b correctly rounded, from y = RN(1/b) (__frcp_rn): Markstein's theorem
-// (IBM J. Res. Develop. 34(1), 1990) -- one FMA correction of RN(a y) gives
-// the correctly rounded quotient for operands in the normal range -- so the
-// result equals a / b bit for bit (checked on all integer a, b <= 4096 and
-// 2e8 random normal operands) at two FMAs and a multiply.
-__device__ __forceinline__ float div_by_rcp(float a, float b, float y)
-{
-  const float q = a * y;
-  return fmaf(fmaf(-q, b, a), y, q);
-}
-
-// image_coords with the reciprocals of w, h, ip[2] and ip[3] given: the same
-// coordinates, for callers that map many pixels of one crop.
-__device__ __forceinline__ bool image_coords_r(const float* ip, const float* vp, int x, int y, float w, float h,
-                                               const float* rcp, float& s, float& t)
-{
-  float u = vp[0] + vp[2] * div_by_rcp((float)x, w, rcp[0]);
-  float v = vp[1] + vp[3] * div_by_rcp((float)y, h, rcp[1]);
-  s = div_by_rcp(u - ip[0], ip[2], rcp[2]) + 0.5f;
-  t = 0.5f - div_by_rcp(v - ip[1], ip[3], rcp[3]);
-  return !(s < 0.0f || t < 0.0f || s > 1.0f || t > 1.0f);
 }
 
 // Whether the reference's multi-level sum() of n elements drops any: only a
@@ -189,6 +181,117 @@ __host__ __device__ inline void moments_merge(Moments& a, const Moments& b)
   a.n = n;
 }
 
+// ---- compensated FP32 sums ----
+// A double-float accumulator, value = h + l: each addition is Knuth's
+// TwoSum (the rounding error of h + x, exact in FP32, is carried in l) and
+// each product is split exactly into its rounded value and the FMA residual
+// x y - RN(x y).  The sums of a tile's pixels then carry ~2^-44 relative
+// error instead of FP32's accumulated ~2^-20.  The _rn intrinsics keep the
+// compiler from contracting or reordering the error terms.
+struct DFs {
+  float h, l;
+};
+
+__device__ __forceinline__ void dfs_add(DFs& a, float x)
+{
+  const float s = __fadd_rn(a.h, x);
+  const float bp = __fsub_rn(s, a.h);
+  const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+  a.h = s;
+  a.l = __fadd_rn(a.l, e);
+}
+
+__device__ __forceinline__ void dfs_add_prod(DFs& a, float x, float y)
+{
+  const float p = __fmul_rn(x, y);
+  dfs_add(a, p);
+  a.l = __fadd_rn(a.l, __fmaf_rn(x, y, -p));
+}
+
+__device__ __forceinline__ void dfs_merge(DFs& a, const DFs& b)
+{
+  dfs_add(a, b.h);
+  a.l = __fadd_rn(a.l, b.l);
+}
+
+// Block-wide sums of N compensated accumulators: a TwoSum butterfly within
+// each warp, then the warps' pairs added in FP64 by N threads.  red: 2 N
+// floats per warp of the block; out (shared): the N sums, visible to every
+// thread on return.
+template <int N>
+__device__ __forceinline__ void block_sum_dfs(DFs (&v)[N], float* red, double* out)
+{
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < N; ++k)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      DFs b = {__shfl_xor_sync(0xffffffffu, v[k].h, o), __shfl_xor_sync(0xffffffffu, v[k].l, o)};
+      dfs_merge(v[k], b);
+    }
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      red[(warp * N + k) * 2] = v[k].h;
+      red[(warp * N + k) * 2 + 1] = v[k].l;
+    }
+  __syncthreads();
+  if (threadIdx.x < N) {
+    double t = 0.0;
+    for (int j = 0; j < nw; ++j) t += (double)red[(j * N + threadIdx.x) * 2] + (double)red[(j * N + threadIdx.x) * 2 + 1];
+    out[threadIdx.x] = t;
+  }
+  __syncthreads();
+}
+
+// Block-wide FP32 sums of N values (a shuffle butterfly per warp, the warps'
+// sums added in FP64 by N threads); out (shared) is visible to every thread
+// on return.  red: N floats per warp.
+template <int N>
+__device__ __forceinline__ void block_sum_f(float (&v)[N], float* red, double* out)
+{
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < N; ++k)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < N; ++k) red[warp * N + k] = v[k];
+  __syncthreads();
+  if (threadIdx.x < N) {
+    double t = 0.0;
+    for (int j = 0; j < nw; ++j) t += (double)red[j * N + threadIdx.x];
+    out[threadIdx.x] = t;
+  }
+  __syncthreads();
+}
+
+// One tile's Moments from its compensated sums: s = (sum mask, sum f, sum g
+// over covered pixels; count, sum f, sum g over mask > 0.5) and the
+// co-moments c = (ff, gg, fg) taken about the FP32 centres (cf, cg).  The
+// exact tile means replace the centres, with the co-moments moved to them
+// (C - n (mean - centre)(mean' - centre')), so the FP64 merge sees exact
+// centred moments whatever the centres' rounding.
+__device__ __forceinline__ Moments tile_moments(const double* s, const double* c, float cf, float cg)
+{
+  Moments p = {s[0], s[1], s[2], s[3], 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (s[3] > 0) {
+    const double n = s[3], mf = s[4] / n, mg = s[5] / n, df = mf - (double)cf, dg = mg - (double)cg;
+    p.mf = mf;
+    p.mg = mg;
+    // sums of squares about the mean: rounding must not leave them below 0
+    // (a tile of equal values gives C = n (mean - centre)^2 up to rounding)
+    const double ff = c[0] - n * df * df, gg = c[1] - n * dg * dg;
+    p.cff = ff < 0.0 ? 0.0 : ff;
+    p.cgg = gg < 0.0 ? 0.0 : gg;
+    p.cfg = c[2] - n * df * dg;
+  }
+  return p;
+}
+
 // gpu::ncc's result from the merged moments (Ncc_kernels.cu:116-134):
 // means over all covered pixels (sum f / sum mask), centred products over
 // mask > 0.5, den < 1e-5 -> 1e5.
@@ -200,6 +303,8 @@ __host__ __device__ inline double moments_ncc(const Moments& m)
   double d1 = m.cff + m.n * ef * ef;
   double d2 = m.cgg + m.n * eg * eg;
   if (m.n == 0) num = d1 = d2 = 0.0;
+  if (d1 < 0.0) d1 = 0.0;  // sums of squares (a NaN stays NaN)
+  if (d2 < 0.0) d2 = 0.0;
   double den = sqrt(d1 * d2);
   if (!(den >= 1e-5)) return den != den ? den : 1e5;
   return num / den;

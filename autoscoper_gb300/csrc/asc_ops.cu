@@ -85,9 +85,11 @@ __global__ void k_image_render(const void* __restrict__ img, int bps, int W, int
 {
   int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= w || y >= h) return;
-  float s, t, r = 0.f;
-  if (image_coords(a.ip, a.vp, x, y, w, h, s, t)) {
-    float v = bilinear(img, bps, W, H, s, t);
+  float ax, ay, r = 0.f;
+  int kx, ky;
+  if (image_axis(a.vp[0], a.vp[2], x, w, a.ip[0], a.ip[2], W, false, kx, ax) &&
+      image_axis(a.vp[1], a.vp[3], y, h, a.ip[1], a.ip[3], H, true, ky, ay)) {
+    float v = bilinear_at(img, bps, W, H, kx, ax, ky, ay);
     r = a.mode == 0 ? 1.0f - v : (a.threshold <= v ? 1.0f : 0.0f);
   }
   out[(size_t)y * w + x] = r;
@@ -265,12 +267,13 @@ __global__ void __launch_bounds__(RB) k_ncc(const float* __restrict__ f, const f
                                             const float* __restrict__ mask, unsigned n, int tree, ReduceScratch sc,
                                             double* __restrict__ result)
 {
-  __shared__ float red[(RB / 32) * 6];
+  __shared__ float red[(RB / 32) * 6 * 2];
+  __shared__ double ds[6], dc[3];
   __shared__ bool last;
   float fv[RE], gv[RE], mv[RE];
   unsigned flags = 0;  // bit k: covered; bit 16+k: covered and mask > 0.5
   const size_t base = (size_t)blockIdx.x * RCHUNK + threadIdx.x;
-  float s[6] = {0, 0, 0, 0, 0, 0};  // sm, sf, sg (covered), n, sf, sg (masked)
+  DFs s[6] = {};  // sm, sf, sg (covered), n, sf, sg (masked)
 #pragma unroll
   for (int k = 0; k < RE; ++k) {
     size_t i = base + (size_t)k * RB;
@@ -280,32 +283,32 @@ __global__ void __launch_bounds__(RB) k_ncc(const float* __restrict__ f, const f
       gv[k] = __ldg(g + i);
       mv[k] = __ldg(mask + i);
       flags |= 1u << k;
-      s[0] += mv[k];
-      s[1] += fv[k];
-      s[2] += gv[k];
+      dfs_add(s[0], mv[k]);
+      dfs_add(s[1], fv[k]);
+      dfs_add(s[2], gv[k]);
       if (mv[k] > 0.5f) {
         flags |= 1u << (16 + k);
-        s[3] += 1.f;
-        s[4] += fv[k];
-        s[5] += gv[k];
+        dfs_add(s[3], 1.f);
+        dfs_add(s[4], fv[k]);
+        dfs_add(s[5], gv[k]);
       }
     }
   }
-  block_sum<6>(s, red);
-  const float cnt = s[3];
-  const float mf = cnt > 0 ? s[4] / cnt : 0.f, mg = cnt > 0 ? s[5] / cnt : 0.f;
-  float c[3] = {0, 0, 0};
+  block_sum_dfs<6>(s, red, ds);
+  const double cnt = ds[3];
+  const float mf = cnt > 0 ? (float)(ds[4] / cnt) : 0.f, mg = cnt > 0 ? (float)(ds[5] / cnt) : 0.f;
+  DFs c[3] = {};
 #pragma unroll
   for (int k = 0; k < RE; ++k)
     if (flags & (1u << (16 + k))) {
       float a = fv[k] - mf, b = gv[k] - mg;
-      c[0] = fmaf(a, a, c[0]);
-      c[1] = fmaf(b, b, c[1]);
-      c[2] = fmaf(a, b, c[2]);
+      dfs_add_prod(c[0], a, a);
+      dfs_add_prod(c[1], b, b);
+      dfs_add_prod(c[2], a, b);
     }
-  block_sum<3>(c, red);
+  block_sum_dfs<3>(c, red, dc);
   if (threadIdx.x == 0) {
-    Moments p = {s[0], s[1], s[2], cnt, mf, mg, c[0], c[1], c[2]};
+    Moments p = tile_moments(ds, dc, mf, mg);
     sc.part[blockIdx.x] = p;
     __threadfence();
     last = atomicAdd(sc.ticket, 1u) == gridDim.x - 1;
@@ -468,12 +471,14 @@ int launch_filter(const asc_filter_desc& f, const float* in, float* out, int w, 
 }
 
 // Per-process reduction scratch sized by asc_ncc_init (the reference keeps
-// module globals too, Ncc_kernels.cu:50-57).
+// module globals too, Ncc_kernels.cu:50-57).  It lives on the device that was
+// current when it was sized; every read or change of it holds g_red_mu.
 static std::mutex g_red_mu;
 static Moments* g_part = nullptr;
 static double* g_means = nullptr;
 static unsigned* g_ticket = nullptr;
 static unsigned g_max_n = 0;
+static int g_red_dev = -1;
 
 std::recursive_mutex& device_gate()
 {
@@ -481,10 +486,28 @@ std::recursive_mutex& device_gate()
   return m;
 }
 
-static int ensure_scratch(unsigned n)
+static int ncc_init_locked(unsigned max_n);
+
+// The scratch for n elements on the current device, copied out under the
+// lock: a thread that grows it frees the old buffers only after taking the
+// lock (and cudaFree waits for the kernels still using them).  Scratch sized
+// on another device is ASC_ERR_STATE: like the reference's module globals it
+// serves one device per process.
+static int ensure_scratch(unsigned n, ReduceScratch* out)
 {
-  if (n <= g_max_n && g_part) return ASC_OK;
-  return asc_ncc_init(n);
+  std::lock_guard<std::mutex> l(g_red_mu);
+  int dev = 0;
+  ASC_CUDA(cudaGetDevice(&dev));
+  if (g_part && dev != g_red_dev) {
+    set_error_message("asc_ncc/asc_hdist: the reduction scratch belongs to another device (asc_ncc_init there)");
+    return ASC_ERR_STATE;
+  }
+  if (!(n <= g_max_n && g_part)) {
+    int rc = ncc_init_locked(n);
+    if (rc) return rc;
+  }
+  *out = ReduceScratch{g_part, g_means, g_ticket};
+  return ASC_OK;
 }
 
 }  // namespace asc
@@ -543,6 +566,11 @@ ASC_API int asc_memcpy_d2h(void* d, const void* s, size_t n, void* st)
 {
   ASC_CUDA(cudaMemcpyAsync(d, s, n, cudaMemcpyDeviceToHost, S(st)));
   ASC_CUDA(cudaStreamSynchronize(S(st)));
+  return ASC_OK;
+}
+ASC_API int asc_memcpy_d2d(void* d, const void* s, size_t n, void* st)
+{
+  ASC_CUDA(cudaMemcpyAsync(d, s, n, cudaMemcpyDeviceToDevice, S(st)));
   return ASC_OK;
 }
 ASC_API int asc_memset(void* d, int v, size_t n, void* st)
@@ -1008,6 +1036,11 @@ ASC_API int asc_sharpen(const float* in, float* out, int w, int h, float radius,
 ASC_API int asc_ncc_init(unsigned max_n)
 {
   std::lock_guard<std::mutex> l(g_red_mu);
+  return ncc_init_locked(max_n);
+}
+
+int asc::ncc_init_locked(unsigned max_n)
+{
   Gate g(device_gate());
   if (g_part) cudaFree(g_part);
   if (g_means) cudaFree(g_means);
@@ -1023,15 +1056,16 @@ ASC_API int asc_ncc_init(unsigned max_n)
   ASC_CUDA(cudaMalloc(&g_ticket, sizeof(unsigned)));
   ASC_CUDA(cudaMemset(g_ticket, 0, sizeof(unsigned)));
   g_max_n = max_n;
+  ASC_CUDA(cudaGetDevice(&g_red_dev));
   return ASC_OK;
 }
 
 ASC_API int asc_ncc(const float* f, const float* g, const float* m, unsigned n, int coverage, double* res, void* st)
 {
   if (!f || !g || !m || !res || n == 0 || (coverage != ASC_SUM_TREE && coverage != ASC_SUM_FULL)) return ASC_ERR_ARG;
-  int rc = ensure_scratch(n);
+  ReduceScratch sc;
+  int rc = ensure_scratch(n, &sc);
   if (rc) return rc;
-  ReduceScratch sc{g_part, g_means, g_ticket};
   int tree = coverage == ASC_SUM_TREE && tree_needed(n);
   k_ncc<<<(n + RCHUNK - 1) / RCHUNK, RB, 0, S(st)>>>(f, g, m, n, tree, sc, res);
   ASC_LAUNCH_CHECK();
@@ -1042,9 +1076,9 @@ ASC_API int asc_hdist(const float* f, const float* g, const float* m, unsigned n
                       void* st)
 {
   if (!f || !g || !m || !res || n == 0 || (coverage != ASC_SUM_TREE && coverage != ASC_SUM_FULL)) return ASC_ERR_ARG;
-  int rc = ensure_scratch(n);
+  ReduceScratch sc;
+  int rc = ensure_scratch(n, &sc);
   if (rc) return rc;
-  ReduceScratch sc{g_part, g_means, g_ticket};
   int tree = coverage == ASC_SUM_TREE && tree_needed(n);
   unsigned nb = (n + RCHUNK - 1) / RCHUNK;
   k_hdist_means<<<nb, RB, 0, S(st)>>>(f, g, m, n, tree, sc);

@@ -68,6 +68,9 @@ int asc_malloc(void **ptr, size_t bytes);
 int asc_free(void *ptr);
 int asc_memcpy_h2d(void *dst, const void *src, size_t bytes, void *stream);
 int asc_memcpy_d2h(void *dst, const void *src, size_t bytes, void *stream);
+/* Device to device, asynchronous: View::filter's copy for an empty or
+ * disabled filter (View.cpp:479-483, :500-517). */
+int asc_memcpy_d2d(void *dst, const void *src, size_t bytes, void *stream);
 int asc_memset(void *dst, int value, size_t bytes, void *stream);
 int asc_stream_sync(void *stream);
 int asc_device_sync(void);
@@ -84,6 +87,13 @@ int asc_host_alloc(void **ptr, size_t bytes);
 int asc_host_free(void *ptr);
 /* Free and total device memory of the current device (cudaMemGetInfo). */
 int asc_mem_info(size_t *free_bytes, size_t *total_bytes);
+/* Read bandwidth of the current device, the denominator of the benchmark's
+ * roofline fractions (no counterpart in the reference): a buffer of `bytes`
+ * (allocated and freed here) is streamed with 16-byte loads that bypass L1,
+ * once to warm up and then `passes` times in one timed launch.  A buffer
+ * well inside L2 measures L2 read bandwidth, one far larger than L2 HBM.
+ * gbs: 1e9 bytes/s read; ms (optional): the timed launch.  Blocking. */
+int asc_probe_read_bandwidth(size_t bytes, int passes, double *gbs, float *ms);
 
 /* ---- volumes ----
  * replaces gpu::VolumeDescription::VolumeDescription(const Volume&)
@@ -183,7 +193,9 @@ int asc_hdist(const float *f, const float *g, const float *mask, unsigned n, int
  * every GPU that loads the library holds until exit (about 288 KiB).
  * n may be at most ASC_NOALLOC_MAX_N elements; larger n returns
  * ASC_ERR_RANGE.  The first call on a device looks up the array's device
- * address, so make that first call before any stream capture.  All calls on
+ * address, so make that first call before any stream capture; the address is
+ * kept per CUDA context, so after a cudaDeviceReset the next call (again
+ * outside any capture) looks it up anew.  All calls on
  * a device share the array: calls that overlap on the GPU (different
  * streams, or a second call issued before the first has finished on another
  * stream) race and must be serialised by the caller. */

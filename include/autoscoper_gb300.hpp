@@ -11,9 +11,14 @@
 //   VolumeDescription    libautoscoper/src/VolumeDescription.hpp:56-84
 //   ncc/hdist/multiply/merge/composite/fill/drr_background/cudaMallocWrap
 //                        gpu/cuda/*_kernels.h, gpu/cuda/CudaWrap.hpp
+//   View                 libautoscoper/src/View.hpp:68-154 (CUDA backend,
+//                        without the OpenGL pixel-buffer members)
 #ifndef AUTOSCOPER_GB300_HPP
 #define AUTOSCOPER_GB300_HPP
 
+#include <algorithm>
+#include <fstream>
+#include <iostream>
 #include <sstream>
 #include <stdexcept>
 #include <string>
@@ -22,6 +27,10 @@
 #include "autoscoper_gb300.h"
 
 namespace xromm {
+// The caller's camera class (libautoscoper/src/Camera.hpp); a View only
+// keeps a pointer to it, as the reference's does.
+class Camera;
+
 namespace gpu {
 
 inline void asc_check(int status, const char* what)
@@ -329,6 +338,216 @@ inline void drr_background(float* src, float* dst, size_t w, size_t h)
 {
   asc_check(asc_drr_background(src, dst, (int)w, (int)h, nullptr), "drr_background");
 }
+
+// ---- View (View.cpp:81-555, CUDA backend) ----
+// One camera's renderers and filter lists, with the view's device scratch
+// (maxWidth x maxHeight floats per buffer, allocated on first use as
+// View::init does).  The OpenGL members (renderDrr(pbo), render(pbo)) are
+// left out: render() writes the RGB composite into a device buffer instead.
+class View
+{
+public:
+  explicit View(Camera& camera) : camera_(&camera), radRenderer_(new RadRenderer()),
+                                  backgroundRenderer_(new BackgroundRenderer())
+  {
+  }
+  ~View()
+  {
+    for (Filter* f : drrFilters_) delete f;
+    for (Filter* f : radFilters_) delete f;
+    for (float* b : drrBuffer_) asc_free(b);
+    for (float* b : {filterBuffer_, drrBufferMerged_, drrFilterBuffer_, radBuffer_, radFilterBuffer_,
+                     backgroundmask_, drr_mask_})
+      asc_free(b);
+    for (RayCaster* r : drrRenderer_) delete r;
+    delete radRenderer_;
+    delete backgroundRenderer_;
+  }
+  View(const View&) = delete;
+  View& operator=(const View&) = delete;
+
+  Camera* camera() { return camera_; }
+  const Camera* camera() const { return camera_; }
+  RayCaster* drrRenderer(int idx) { return drrRenderer_[idx]; }
+  const RayCaster* drrRenderer(int idx) const { return drrRenderer_[idx]; }
+  RadRenderer* radRenderer() { return radRenderer_; }
+  const RadRenderer* radRenderer() const { return radRenderer_; }
+  std::vector<Filter*>& drrFilters() { return drrFilters_; }
+  const std::vector<Filter*>& drrFilters() const { return drrFilters_; }
+  std::vector<Filter*>& radFilters() { return radFilters_; }
+  const std::vector<Filter*>& radFilters() const { return radFilters_; }
+  BackgroundRenderer* backgroundRenderer() { return backgroundRenderer_; }
+  unsigned int nbDrrRenderer() const { return (unsigned)drrRenderer_.size(); }
+
+  void addDrrRenderer()
+  {
+    drrRenderer_.push_back(new RayCaster());
+    drrBuffer_.push_back(nullptr);
+  }
+
+  // RadRenderer into the view's buffer, then the radiograph filters (View.cpp:147-169)
+  void renderRad(float* buffer, unsigned width, unsigned height)
+  {
+    init();
+    clamp_size(width, height, "renderRad");
+    radRenderer_->render(radBuffer_, width, height);
+    filter(radFilters_, radBuffer_, buffer, width, height);
+  }
+
+  // The background mask, or nothing while the threshold is negative (View.cpp:171-194)
+  void renderBackground(float* buffer, unsigned width, unsigned height)
+  {
+    if (backgroundThreshold_ < 0.0f) return;
+    init();
+    clamp_size(width, height, "renderBackground");
+    backgroundRenderer_->render(buffer, width, height, backgroundThreshold_);
+  }
+
+  // mask = filtered DRR != 0 (View.cpp:196-199)
+  void renderDRRMask(float* in_buffer, float* out_buffer, unsigned width, unsigned height)
+  {
+    drr_background(in_buffer, out_buffer, width, height);
+  }
+
+  // Every volume's DRR, merged (sum clamped to 1), then the DRR filters (View.cpp:201-231)
+  void renderDrr(float* buffer, unsigned width, unsigned height)
+  {
+    init();
+    clamp_size(width, height, "renderDrr");
+    asc_check(asc_memset(drrBufferMerged_, 0, (size_t)width * height * sizeof(float), nullptr), "View::renderDrr");
+    for (size_t i = 0; i < drrRenderer_.size(); ++i) {
+      drrRenderer_[i]->render(drr_buffer(i), width, height);
+      merge(drrBufferMerged_, drrBuffer_[i], drrBufferMerged_, width, height);
+    }
+    filter(drrFilters_, drrBufferMerged_, buffer, width, height);
+  }
+
+  // One volume's DRR, then the DRR filters (View.cpp:233-256)
+  void renderDrrSingle(int volume, float* buffer, unsigned width, unsigned height)
+  {
+    init();
+    clamp_size(width, height, "renderDrrSingle");
+    drrRenderer_[volume]->render(drr_buffer(volume), width, height);
+    filter(drrFilters_, drrBuffer_[volume], buffer, width, height);
+  }
+
+  // The display composite (View.cpp:352-380) into a device buffer of
+  // 3 x width x height floats: R = DRR, G = mask (DRR + rad) / 2, B = rad.
+  void render(float* rgb, unsigned width, unsigned height)
+  {
+    init();
+    clamp_size(width, height, "render");
+    const size_t bytes = (size_t)width * height * sizeof(float);
+    if (drr_enabled)
+      renderDrr(drrFilterBuffer_, width, height);
+    else
+      asc_check(asc_memset(drrFilterBuffer_, 0, bytes, nullptr), "View::render");
+    if (rad_enabled)
+      renderRad(radFilterBuffer_, width, height);
+    else
+      asc_check(asc_memset(radFilterBuffer_, 0, bytes, nullptr), "View::render");
+    renderBackground(backgroundmask_, width, height);
+    renderDRRMask(drrFilterBuffer_, drr_mask_, width, height);
+    composite(drrFilterBuffer_, radFilterBuffer_, backgroundmask_, drr_mask_, rgb, width, height);
+  }
+
+  // The merged, filtered DRR as an ASCII PGM, 255 (1 - value), rows bottom
+  // up (View.cpp:258-334)
+  void saveImage(const std::string& filename, int width, int height)
+  {
+    unsigned w = (unsigned)width, h = (unsigned)height;
+    init();
+    clamp_size(w, h, "saveImage");
+    renderDrr(drrFilterBuffer_, w, h);
+    std::vector<float> img((size_t)w * h);
+    asc_check(asc_memcpy_d2h(img.data(), drrFilterBuffer_, img.size() * sizeof(float), nullptr), "View::saveImage");
+    std::ofstream file(filename.c_str(), std::ios::out);
+    file << "P2" << std::endl << w << " " << h << std::endl << 255 << std::endl;
+    for (unsigned y = 0; y < h; ++y)
+      for (unsigned x = 0; x < w; ++x)
+        file << (int)(unsigned char)(int)(255 * (1.0 - img[(size_t)(h - y - 1) * w + x])) << " ";
+  }
+
+  // BackgroundRenderer::set_back with a host float image (View.cpp:423-426)
+  void updateBackground(const float* buffer, unsigned width, unsigned height)
+  {
+    backgroundRenderer_->set_back(buffer, width, height);
+  }
+  void setBackgroundThreshold(float threshold) { backgroundThreshold_ = threshold; }
+
+  bool drr_enabled = true;
+  bool rad_enabled = true;
+
+private:
+  // View::init (View.cpp:428-445): the view's scratch, masks filled with 1
+  void init()
+  {
+    if (filterBuffer_) return;
+    const size_t bytes = maxWidth_ * maxHeight_ * sizeof(float);
+    for (float** p : {&filterBuffer_, &drrBufferMerged_, &drrFilterBuffer_, &radBuffer_, &radFilterBuffer_,
+                      &backgroundmask_, &drr_mask_})
+      cudaMallocWrap(*p, bytes);
+    fill(backgroundmask_, (unsigned)(maxWidth_ * maxHeight_), 1.0f);
+    fill(drr_mask_, (unsigned)(maxWidth_ * maxHeight_), 1.0f);
+  }
+
+  // A volume's DRR buffer (a renderer added after init gets one on first use)
+  float* drr_buffer(size_t i)
+  {
+    if (!drrBuffer_[i]) cudaMallocWrap(drrBuffer_[i], maxWidth_ * maxHeight_ * sizeof(float));
+    return drrBuffer_[i];
+  }
+
+  void clamp_size(unsigned& width, unsigned& height, const char* who) const
+  {
+    if (width > maxWidth_ || height > maxHeight_)
+      std::cerr << "View::" << who << "(): ERROR: Buffer too large." << std::endl;
+    width = std::min<unsigned>(width, (unsigned)maxWidth_);
+    height = std::min<unsigned>(height, (unsigned)maxHeight_);
+  }
+
+  // View::filter (View.cpp:475-518): the enabled filters in order, ping-pong
+  // between `output` and the view's filter buffer so that the last one
+  // writes `output`; a disabled filter copies, an empty list copies.
+  void filter(const std::vector<Filter*>& filters, const float* input, float* output, unsigned width,
+              unsigned height)
+  {
+    const size_t bytes = (size_t)width * height * sizeof(float);
+    if (filters.empty()) {
+      asc_check(asc_memcpy_d2d(output, input, bytes, nullptr), "View::filter");
+      return;
+    }
+    float* b1 = filters.size() % 2 ? output : filterBuffer_;
+    float* b2 = filters.size() % 2 ? filterBuffer_ : output;
+    if (filters[0]->enabled())
+      filters[0]->apply(input, b1, (int)width, (int)height);
+    else
+      asc_check(asc_memcpy_d2d(b1, input, bytes, nullptr), "View::filter");
+    for (size_t i = 1; i < filters.size(); ++i) {
+      if (filters[i]->enabled())
+        filters[i]->apply(b1, b2, (int)width, (int)height);
+      else
+        asc_check(asc_memcpy_d2d(b2, b1, bytes, nullptr), "View::filter");
+      std::swap(b1, b2);
+    }
+  }
+
+  Camera* camera_;
+  std::vector<RayCaster*> drrRenderer_;
+  RadRenderer* radRenderer_;
+  BackgroundRenderer* backgroundRenderer_;
+  std::vector<Filter*> drrFilters_, radFilters_;
+  size_t maxWidth_ = 3000, maxHeight_ = 3000;
+  std::vector<float*> drrBuffer_;
+  float* drrBufferMerged_ = nullptr;
+  float* drrFilterBuffer_ = nullptr;
+  float* radBuffer_ = nullptr;
+  float* radFilterBuffer_ = nullptr;
+  float* filterBuffer_ = nullptr;
+  float* backgroundmask_ = nullptr;
+  float* drr_mask_ = nullptr;
+  float backgroundThreshold_ = -1.0f;
+};
 
 }  // namespace gpu
 }  // namespace xromm

@@ -11,8 +11,9 @@ import pytest
 
 from autoscoper_gb300 import formats as F, geometry as G, scene as S
 import trial_files
+from oracle.ref import REFERENCE_ROOT
 
-SAMPLE = "/root/reference/sample_data"
+SAMPLE = os.path.join(REFERENCE_ROOT, "sample_data")
 
 
 @pytest.mark.parametrize("compression", ["none", "packbits", "lzw"])
@@ -146,4 +147,5 @@ def test_trial_from_files_on_the_engine(tmp_path):
     cost, vcost = eng.eval(np.zeros(2, np.int32), man)
     for k in range(2):
         want = tr.track_frame(0, tr.compose(0, man[k]))
-        assert np.allclose(vcost[k], want, rtol=1e-5, atol=2e-6)
+        for got, c in zip(vcost[k], want):  # the NCC bar per view
+            assert abs(got - c) <= 1e-5 * max(abs(1.0 - c), 1e-2), (got, c)

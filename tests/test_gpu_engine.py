@@ -1,6 +1,8 @@
 """GPU parity of the batched engine and of the plain per-pose path against
-the FP64 oracle's Tracker::minimizationFunc, at the stated tolerance: NCC
-cost within 1e-5 relative (plus 2e-6 absolute for FP32 image rounding)."""
+the FP64 oracle's Tracker::minimizationFunc, at the NCC bar: each view's NCC
+within 1e-5 relative, 1e-7 absolute where |NCC| < 0.01 (FP32 image rounding
+leaves ~1e-8 of NCC per stage); a cost, the sum over views of 1 - NCC,
+within the sum of its views' bars.  SAD costs within 1e-5 relative."""
 import numpy as np
 import pytest
 
@@ -10,7 +12,13 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-TOL_REL, TOL_ABS = 1e-5, 2e-6
+TOL_REL = 1e-5
+NCC_FLOOR = 1e-2  # below |NCC| = 0.01 the bar is the absolute TOL_REL * NCC_FLOOR
+TOL_ABS_SAD = 2e-6  # SAD costs: FP32 tile partials of |(f - mF) - (g - mG)|
+
+
+def ncc_bar(ncc):
+    return TOL_REL * max(abs(ncc), NCC_FLOOR)
 
 
 def make_targets(sc, tr):
@@ -40,9 +48,11 @@ def _cands(rng, n, nb, spread=2.0):
     return bones, man
 
 
-def _check(got, ref):
-    """A two-view cost: the sum of two terms each within the NCC bar."""
-    assert abs(got - ref) <= 2 * TOL_REL * max(1.0, abs(ref)) + TOL_ABS, (got, ref)
+def _check(got, ref, refv):
+    """A cost against the oracle's: within the sum of its views' NCC bars
+    (refv: the oracle's per-view terms 1 - NCC; a 9999 term is exact)."""
+    bar = sum(ncc_bar(1.0 - c) if c != 9999.0 else 0.0 for c in refv)
+    assert abs(got - ref) <= bar, (got, ref, bar)
 
 
 @pytest.mark.parametrize("coverage", [L.ASC_SUM_TREE, L.ASC_SUM_FULL])
@@ -56,14 +66,14 @@ def test_engine_and_plain_match_oracle(scene, coverage):
     pcost, pvcost = eng.eval(bones, man, plain=True)
     for k in range(len(bones)):
         ref = tr.minimization_func(int(bones[k]), man[k])
-        # cost = sum over views of (1 - NCC): each term within the NCC bar
-        assert abs(cost[k] - ref) <= 2 * TOL_REL * max(1.0, abs(ref)) + TOL_ABS, (cost[k], ref)
-        assert abs(pcost[k] - ref) <= 2 * TOL_REL * max(1.0, abs(ref)) + TOL_ABS, (pcost[k], ref)
         refv = tr.track_frame(int(bones[k]), tr.compose(int(bones[k]), man[k]))
+        # cost = sum over views of (1 - NCC): each term within the NCC bar
+        _check(cost[k], ref, refv)
+        _check(pcost[k], ref, refv)
         for v in range(2):
             for got in (vcost[k, v], pvcost[k, v]):
                 n_got, n_ref = 1.0 - got, 1.0 - refv[v]
-                assert abs(n_got - n_ref) <= TOL_REL * max(abs(n_ref), 1e-3) + TOL_ABS, (n_got, n_ref)
+                assert abs(n_got - n_ref) <= ncc_bar(n_ref), (n_got, n_ref)
 
 
 @pytest.mark.parametrize("coverage", [L.ASC_SUM_TREE, L.ASC_SUM_FULL])
@@ -86,11 +96,11 @@ def test_engine_sad_cost_model_matches_oracle(scene, coverage):
         ref = tr.minimization_func(int(bones[k]), man[k])
         assert ref == pytest.approx(sum(refv))
         for got in (cost[k], pcost[k]):
-            assert abs(got - ref) <= TOL_REL * abs(ref) + TOL_ABS, (got, ref)
+            assert abs(got - ref) <= TOL_REL * abs(ref) + TOL_ABS_SAD, (got, ref)
         for v in range(2):
             assert refv[v] > 0
             for got in (vcost[k, v], pvcost[k, v]):
-                assert abs(got - refv[v]) <= TOL_REL * refv[v] + TOL_ABS, (k, v, got, refv[v])
+                assert abs(got - refv[v]) <= TOL_REL * refv[v] + TOL_ABS_SAD, (k, v, got, refv[v])
     assert np.all(vcost[-1] == 9999.0)
     # the batch is order independent in this mode too
     perm = rng.permutation(len(bones))
@@ -104,7 +114,7 @@ def test_engine_out_of_view_penalty(scene):
     man = np.array([[0, 0, 0, 0, 0, 0], [900.0, 0, 0, 0, 0, 0], [0, 0, 5000.0, 0, 0, 0]])
     cost, vcost = eng.eval(np.zeros(3, np.int32), man)
     for k in range(3):
-        _check(cost[k], tr.minimization_func(0, man[k]))
+        _check(cost[k], tr.minimization_func(0, man[k]), tr.track_frame(0, tr.compose(0, man[k])))
     assert cost[2] == 2 * 9999.0 and np.all(vcost[2] == 9999.0)  # Tracker.cpp:614-617
 
 
@@ -154,7 +164,8 @@ def test_engine_golden_reference_values():
         cost, vcost = eng.eval(np.zeros(1, np.int32), np.zeros((1, 6)))
         for vi in range(2):
             ref_ncc = float(z[f"v{vi}p{k}_ncc"])  # reference kernels, float
-            assert abs((1.0 - vcost[0, vi]) - ref_ncc) < 5e-4
+            # the NCC bar: 1e-5 relative, 1e-7 absolute below |NCC| = 0.01
+            assert abs((1.0 - vcost[0, vi]) - ref_ncc) <= 1e-5 * max(abs(ref_ncc), 1e-2), (vi, k, ref_ncc)
 
 
 def test_pso_converges():
@@ -170,7 +181,7 @@ def test_pso_converges():
     for b in range(2):
         c0 = tr.minimization_func(b, np.zeros(6))
         assert cost[b] < c0
-        _check(cost[b], tr.minimization_func(b, best[b]))
+        _check(cost[b], tr.minimization_func(b, best[b]), tr.track_frame(b, tr.compose(b, best[b])))
     # the stall rule stops each swarm once its gBest stops moving
     best2, cost2, ev2 = eng.pso(n_particles=48, n_iter=400, lo=-3, hi=3, seed=3, max_stall=3)
     its = eng.last_pso_iterations
@@ -178,7 +189,7 @@ def test_pso_converges():
     assert 48 * its <= ev2 <= 2 * 48 * its
     for b in range(2):
         assert cost2[b] < tr.minimization_func(b, np.zeros(6))
-        _check(cost2[b], tr.minimization_func(b, best2[b]))
+        _check(cost2[b], tr.minimization_func(b, best2[b]), tr.track_frame(b, tr.compose(b, best2[b])))
 
 
 def test_hidden_bone_scores_the_empty_mask(scene):

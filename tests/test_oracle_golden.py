@@ -35,9 +35,12 @@ def test_views_against_reference_outputs():
             rad = O.image_render(v.radiograph, np.float32(v.camera.viewport).astype(np.float64),
                                  np.float32(vp).astype(np.float64), w, h)
             assert np.abs(rad - z[key + "_rad"]).max() < 2e-5
-            # NCC / SAD of the reference's own masked images through the oracle
+            # the oracle's NCC against the reference's own FP32 NCC (its float
+            # tree sums), which holds the NCC bar on these fixtures: 1e-5
+            # relative, 1e-7 absolute below 0.01
             ncc = 1.0 - tr.track_frame(0, pose)[vi]
-            assert abs(ncc - float(z[key + "_ncc"])) < 5e-4
+            ref_ncc = float(z[key + "_ncc"])
+            assert abs(ncc - ref_ncc) <= 1e-5 * max(abs(ref_ncc), 1e-2), (vi, k, ncc, ref_ncc)
 
 
 def test_filters_against_reference_outputs():
