@@ -42,27 +42,60 @@ static __device__ __align__(256) unsigned char g_noalloc[kPartBytes + 2 * sizeof
 
 struct Slot {
   void* base = nullptr;
+  unsigned long long ctx = 0;  // unique id of the context the address belongs to
   bool ready = false;
 };
 std::mutex g_mu;
 Slot g_slots[64];  // one per device ordinal
 
-// Device address of g_noalloc on the current device.  The first call on a
-// device looks it up (cudaGetSymbolAddress with that device current); later
-// calls reuse it.
+// cuCtxGetId of the driver, reached through the runtime (no link against
+// libcuda): the id of the current context, unique for the life of the
+// process, so a context created anew on a device (after a cudaDeviceReset by
+// the host) never matches an address looked up in the one before it.
+typedef int (*CtxGetIdFn)(void* ctx, unsigned long long* id);
+CtxGetIdFn ctx_get_id()
+{
+  static CtxGetIdFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return (CtxGetIdFn)p;
+  }();
+  return fn;
+}
+
+bool current_ctx_id(unsigned long long* id)
+{
+  CtxGetIdFn fn = ctx_get_id();
+  return fn && fn(nullptr, id) == 0;
+}
+
+// Device address of g_noalloc in the current device's current context.  The
+// first call in a context looks it up (cudaGetSymbolAddress with that device
+// current); later calls in the same context reuse it.  Where the driver
+// cannot name the context, every call looks the address up.
 int noalloc_base(void** out)
 {
   int dev = 0;
   ASC_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return ASC_ERR_RANGE;
+  unsigned long long ctx = 0;
+  bool known = current_ctx_id(&ctx);
   std::lock_guard<std::mutex> lock(g_mu);
   Slot& s = g_slots[dev];
-  if (!s.ready) {
+  if (!s.ready || !known || s.ctx != ctx) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc);
-    if (e != cudaSuccess) return cuda_status(e);
+    if (e != cudaSuccess) {
+      s.ready = false;
+      return cuda_status(e);
+    }
+    if (!known) known = current_ctx_id(&ctx);  // the lookup made the runtime's context current
     s.base = p;
-    s.ready = true;
+    s.ctx = ctx;
+    s.ready = known;
   }
   *out = s.base;
   return ASC_OK;

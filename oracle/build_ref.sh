@@ -6,9 +6,10 @@
 # (k<<<cfg>>>(...)) are rewritten on the fly by sed into the stand-in's
 # launcher; nothing is written outside oracle/_ref.  Used only to pin the
 # oracle (tests/test_oracle_pin.py, tests/golden/make_golden.py).
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh REFERENCE_ROOT   (oracle/ref.py passes it)
 set -e
-REF=${1:-/root/reference}
+[ $# -ge 1 ] || { echo "usage: $0 REFERENCE_ROOT" >&2; exit 2; }
+REF=$1
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 SRC="$REF/libautoscoper/src"

@@ -16,6 +16,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SO = os.path.join(HERE, "_ref", "libascref.so")
+# Where the reference checkout lies on the machine that builds the pin: the
+# ASC_REFERENCE_ROOT environment variable, else the build container's copy.
 REFERENCE_ROOT = os.environ.get("ASC_REFERENCE_ROOT", "/root/reference")
 _LIB = None
 

@@ -3,7 +3,8 @@ device memory (an application that keeps a fixed device-memory budget, or a
 loop that cannot pay cudaMalloc's device-wide synchronisation).  Called
 through the C ABI, it must return what asc_ncc returns for the same inputs,
 on two calls in a row (the shared fixed array keeps the previous call's
-contents), and reject sizes above ASC_NOALLOC_MAX_N.
+contents), agree with the FP64 oracle's NCC within the NCC bar (1e-5
+relative), and reject sizes above ASC_NOALLOC_MAX_N.
 
 The file name makes pytest collect it after every other test file."""
 import ctypes as C
@@ -13,11 +14,13 @@ import pytest
 
 from autoscoper_gb300 import _lib as L
 from autoscoper_gb300 import api
+from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
 ASC_NOALLOC_MAX_N = 1 << 24
 TOL = 1e-12  # same kernel and same summation order as asc_ncc
+TOL_ORACLE = 1e-5  # the NCC bar against the FP64 oracle, relative
 
 
 def _inputs(n, seed):
@@ -45,6 +48,8 @@ def test_noalloc_matches_ncc_twice(coverage):
         want = _result(lib, "asc_ncc", df, dg, dm, n, coverage)
         got = _result(lib, "asc_ncc_noalloc", df, dg, dm, n, coverage)
         assert abs(got - want) <= TOL * max(1.0, abs(want)), (call, got, want)
+        ref = O.ncc(f, g, m, tree=coverage == L.ASC_SUM_TREE)
+        assert abs(got - ref) <= TOL_ORACLE * abs(ref), (call, got, ref)
 
 
 def test_noalloc_rejects_oversize():
