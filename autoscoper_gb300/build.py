@@ -26,7 +26,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
          "--expt-relaxed-constexpr",
          "-I" + os.path.join(ROOT, "include")]
-SOURCES = ["asc_ops.cu", "asc_engine.cu", "asc_host.cu", "asc_noalloc.cu", "asc_optimize.cu", "asc_curves.cu"]
+SOURCES = ["asc_ops.cu", "asc_engine.cu", "asc_host.cu", "asc_noalloc.cu", "asc_optimize.cu", "asc_curves.cu",
+           "asc_probe.cu"]
 
 
 def nvcc() -> str:

@@ -105,6 +105,74 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def profile_counts(kernel):
+    """Per-launch counters of `kernel` from the committed ncu summary of the
+    bench's roofline batch (profiles/<kernel>_counters_batch_300.json), or None."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_counters_batch_300.json")
+    return json.load(open(p)) if os.path.exists(p) else None
+
+
+def device_sms():
+    import torch
+    return torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+
+
+def roofline(phase, samples, pixels, marched, slots, sm_mhz):
+    """The dominant kernel (k_ray) against the limit it is bound by.
+
+    k_ray marches FP32 samples whose taps come from L1/L2 (every volume is
+    far below the 129 MB L2); ncu shows it bound by instruction issue.  So
+    `frac` is the issue fraction: warp instructions per launch (ncu,
+    profiles/k_ray_counters_batch_300.json, scaled to this launch by marched
+    samples) over SMs x 4 schedulers x the sampled SM clock x the launch's
+    CUDA-event time.  Beside it: the marched gather bytes (16 B per marched
+    sample + 4 B per DRR pixel) against the L2 read bandwidth measured here
+    (frac_l2), the DRAM traffic against the HBM copy peak (frac_hbm), and the
+    algorithmic bytes of the reference's march (16 B per sample of the whole
+    box + 4 B per pixel) under alg_* (above the L2 peak: empty-space skipping
+    proves most of those samples add 0 and never loads them).  k_view's issue
+    and DRAM fractions ride along."""
+    from autoscoper_gb300 import _lib as L
+    import ctypes as C
+    hbm, peak_kind = peaks()
+    g = C.c_double()
+    L.call("asc_probe_read_bandwidth", 32 << 20, 400, C.byref(g), None)
+    l2 = g.value
+    sms = device_sms()
+    clk = (sm_mhz or 2070.0) * 1e6
+    out = {"bound": "issue", "kernel": "k_ray", "unit": "G warp-inst/s"}
+    ray_s, view_s = phase[1] / 1e3, phase[2] / 1e3
+    issue_peak = sms * 4 * clk
+    kr = profile_counts("k_ray")
+    if kr and kr.get("marched_per_launch"):
+        inst = kr["inst_per_launch"] * marched / kr["marched_per_launch"]
+        out.update(achieved=inst / ray_s / 1e9, peak=issue_peak / 1e9, frac=inst / ray_s / issue_peak,
+                   inst_per_launch=inst)
+        traffic = kr["dram_bytes_per_launch"] * marched / kr["marched_per_launch"]
+    else:
+        out.update(achieved=None, peak=issue_peak / 1e9, frac=None)
+        traffic = None
+    out["frac_issue"] = out["frac"]
+    marched_bytes = 16.0 * marched + 4.0 * pixels
+    out.update(l2_peak_gbs=l2, achieved_marched_gbs=marched_bytes / ray_s / 1e9,
+               frac_l2=marched_bytes / ray_s / 1e9 / l2, traffic=traffic, hbm_peak_gbs=hbm, peak_kind=peak_kind,
+               frac_hbm=traffic / ray_s / 1e9 / hbm if traffic else None)
+    alg = 16.0 * samples + 4.0 * pixels
+    out.update(alg_bytes_per_launch=alg, alg_gbs=alg / ray_s / 1e9, alg_over_l2_peak=alg / ray_s / 1e9 / l2,
+               marched_fraction=marched / max(samples, 1), simt_efficiency=marched / max(slots, 1),
+               sm_mhz=clk / 1e6, sms=sms)
+    kv = profile_counts("k_view")
+    if kv and kv.get("pixels_per_launch"):
+        vi = kv["inst_per_launch"] * pixels / kv["pixels_per_launch"]
+        vt = kv["dram_bytes_per_launch"] * pixels / kv["pixels_per_launch"]
+        out["k_view"] = {"ms": phase[2], "frac_issue": vi / view_s / issue_peak, "traffic": vt,
+                         "frac_hbm": vt / view_s / 1e9 / hbm}
+    out["note"] = ("frac = k_ray's issued warp instructions / (SMs x 4 x SM clock x time); the taps come from "
+                   "L1/L2, so frac_l2 (marched gather bytes / measured L2 read bandwidth) and frac_hbm (DRAM traffic "
+                   "/ HBM copy peak) show the memory side; alg_* is the reference march's algorithmic bytes")
+    return out
+
+
 def dist_setup():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -284,19 +352,7 @@ def main():
     cnt = (C.c_ulonglong * 4)()
     L.call("asc_engine_counters", eng.handle, cnt)
     marched, slots = cnt[2], cnt[3]
-    ray_ms = phase[1]
-    # k_ray's algorithmic bytes: 8 u16 taps (16 B) per trilinear sample of the
-    # reference's march (far to near through the whole box) + the 4 B DRR write
-    alg_bytes = 16.0 * samples.value + 4.0 * pixels.value
-    achieved = alg_bytes / (ray_ms / 1000.0) / 1e9
-    marched_gbs = (16.0 * marched + 4.0 * pixels.value) / (ray_ms / 1000.0) / 1e9
-    peak, peak_kind = peaks()
-    traffic_path = os.path.join(ROOT, "profiles", "k_ray_traffic.json")
-    traffic = None
-    if os.path.exists(traffic_path):
-        t = json.load(open(traffic_path))
-        if t.get("samples_per_launch"):  # scale the captured launch to this one by samples
-            traffic = t["dram_bytes_per_launch"] * samples.value / t["samples_per_launch"]
+    rl = roofline(phase, samples.value, pixels.value, marched, slots, clk.summary().get("sm_mhz"))
     # ---- plain per-pose drop-in form on the same GPU (sampled)
     plain_v = None
     if not args.no_plain:
@@ -319,17 +375,7 @@ def main():
                 "config": dict(CONFIG, l2="256 MB memset between timed steps", parallelism=f"replicas x{ws}"),
                 "e2e": {"value": e2e, "unit": "pose-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "gpu_launches": args.steps * (1 + 5 * iters),
-                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": traffic,
-                             "kernel": "k_ray", "peak_kind": peak_kind,
-                             "marched_fraction": marched / max(samples.value, 1),
-                             "achieved_marched": marched_gbs, "frac_marched": marched_gbs / peak,
-                             "simt_efficiency": marched / max(slots, 1),
-                             "note": "achieved: 16 B (8 u16 taps) per sample of the reference's march + 4 B DRR "
-                                     "write per pixel, per k_ray launch; empty-space skipping marches "
-                                     "marched_fraction of those samples (the others provably add 0); the taps "
-                                     "are served from L1/L2 (volumes <= 10 MB), so HBM is not the binding "
-                                     "limit: the kernel is issue-bound"},
+                "roofline": rl,
                 "kernel_ms": {"setup": phase[0], "ray": phase[1], "view": phase[2]},
                 "work": {"samples_per_batch": samples.value, "marched_per_batch": marched,
                          "pixels_per_batch": pixels.value, "batch": nb * npart},
@@ -490,6 +536,65 @@ def run_precision(args):
             "data": "batched PSO workload (3 bones, 2 views 1024^2, chain filters), synthetic"}
 
 
+def run_config1(args):
+    """The plain method, small: one bone (128^3 u16 phantom at 0.5 mm), 2
+    views of 512^2, Sobel, Downhill Simplex from +-2 mm / +-2 deg, one frame.
+    Reports the plain per-pose form (the reference's launch sequence, one
+    pose at a time), the batched engine on a 256-candidate batch, the
+    simplex registration end to end, and the FP64 oracle on the host cores."""
+    import ctypes as C
+    from autoscoper_gb300 import _lib as L, api, scene as S
+    L.load()
+    sc = S.make_scene([(128, 128, 128)], 0.5, (512, 512), 0.4, filters="sobel", seed=1, bone_offsets=[(0, 0, 0)])
+    vols = api.render_targets(sc)
+    rng = np.random.Generator(np.random.PCG64(77))
+    sc.poses = [S.perturb(t, rng, 2.0, 2.0) for t in sc.truth]
+    eng = api.Engine(sc, max_items=256, volumes=vols)
+    crng = np.random.default_rng(4)
+    n = 256
+    bones = np.zeros(n, np.int32)
+    man = np.concatenate([crng.uniform(-2, 2, (n, 3)), crng.uniform(-2, 2, (n, 3))], 1)
+    for _ in range(3):
+        eng.eval(bones, man)
+    L.call("asc_device_sync")
+    t0 = time.perf_counter()
+    reps = 10
+    for _ in range(reps):
+        eng.eval(bones, man)
+    batched = reps * n / (time.perf_counter() - t0)
+    eng.eval(bones[:4], man[:4], plain=True)
+    lat = []
+    for k in range(64):
+        t1 = time.perf_counter()
+        eng.eval(bones[k:k + 1], man[k:k + 1], plain=True)
+        lat.append(time.perf_counter() - t1)
+    lat = np.array(lat)
+    regs = []
+    srng = np.random.Generator(np.random.PCG64(78))
+    for f in range(min(args.frames, 10)):
+        eng.set_base_pose(0, S.perturb(sc.truth[0], srng, 2.0, 2.0))
+        t1 = time.perf_counter()
+        poses, cost, ev = eng.optimize_frame(method=1)
+        dt = time.perf_counter() - t1
+        err = np.abs(poses[0] - np.asarray(sc.truth[0]))
+        regs.append({"s": dt, "evals": ev, "err_mm": float(err[:3].max()), "err_deg": float(err[3:].max())})
+    from oracle import oracle as O
+    tr = O.Tracker(sc)
+    t1 = time.perf_counter()
+    for k in range(3):
+        tr.minimization_func(0, man[k])
+    cpu = 3 / (time.perf_counter() - t1)
+    return {"workload": "config 1: plain method, one 128^3 u16 bone at 0.5 mm, 2 views 512^2, Sobel, simplex",
+            "metric": "pose evals/s (DRR+filter+NCC, 2 views)", "unit": "pose-evals/s",
+            "plain": {"value": 1.0 / lat.mean(), "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                      "p99_ms": 1e3 * float(np.percentile(lat, 99))},
+            "batched": {"value": batched, "batch": n, "speedup_vs_plain": batched * lat.mean()},
+            "simplex_registration": regs,
+            "cpu_baseline": {"value": cpu, "unit": "pose-evals/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": "3 minimizationFunc evaluations by the FP64 oracle"},
+            "data": "synthetic phantom and radiographs rendered at a seeded ground truth"}
+
+
 def run_roofline(args):
     """The roofline batch alone: `--particles` candidates per bone of the
     default workload at fixed random manipulators, evaluated `--reps` times
@@ -523,7 +628,7 @@ def run_roofline(args):
 
 
 if __name__ == "__main__":
-    if len(sys.argv) > 1 and sys.argv[1] in ("tracking", "serving", "precision", "roofline"):
+    if len(sys.argv) > 1 and sys.argv[1] in ("tracking", "serving", "precision", "roofline", "config1"):
         ap = argparse.ArgumentParser()
         ap.add_argument("workload")
         ap.add_argument("--frames", type=int, default=20)
@@ -538,7 +643,7 @@ if __name__ == "__main__":
                         help="roofline: volume storage")
         a = ap.parse_args()
         fn = {"tracking": run_tracking, "serving": run_serving, "precision": run_precision,
-              "roofline": run_roofline}[a.workload]
+              "roofline": run_roofline, "config1": run_config1}[a.workload]
         print(json.dumps(fn(a)), flush=True)
     else:
         main()
