@@ -80,16 +80,31 @@ struct ImgArgs {
   int mode;  // 0 radiograph, 1 background mask
 };
 
-__global__ void k_image_render(const void* __restrict__ img, int bps, int W, int H, ImgArgs a, float* __restrict__ out,
-                               int w, int h)
+__global__ void __launch_bounds__(256) k_image_render(const void* __restrict__ img, int bps, int W, int H, ImgArgs a,
+                                                      float* __restrict__ out, int w, int h)
 {
-  int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  // the film-plane mapping of the block's 32 columns and 8 rows, in FP64
+  // (image_axis), shared by its pixels
+  __shared__ int s_k[40];
+  __shared__ float s_a[40];
+  const int t = threadIdx.y * 32 + threadIdx.x;
+  if (t < 40) {
+    const bool row = t >= 32;
+    const int j = row ? blockIdx.y * 8 + (t - 32) : blockIdx.x * 32 + t;
+    int k = 0;
+    float wgt = 0.f;
+    const bool ok = row ? j < h && image_axis(a.vp[1], a.vp[3], j, h, a.ip[1], a.ip[3], H, true, k, wgt)
+                        : j < w && image_axis(a.vp[0], a.vp[2], j, w, a.ip[0], a.ip[2], W, false, k, wgt);
+    s_k[t] = ok ? k : INT_MIN;
+    s_a[t] = wgt;
+  }
+  __syncthreads();
+  int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
   if (x >= w || y >= h) return;
-  float ax, ay, r = 0.f;
-  int kx, ky;
-  if (image_axis(a.vp[0], a.vp[2], x, w, a.ip[0], a.ip[2], W, false, kx, ax) &&
-      image_axis(a.vp[1], a.vp[3], y, h, a.ip[1], a.ip[3], H, true, ky, ay)) {
-    float v = bilinear_at(img, bps, W, H, kx, ax, ky, ay);
+  const int kx = s_k[threadIdx.x], ky = s_k[32 + threadIdx.y];
+  float r = 0.f;
+  if (kx != INT_MIN && ky != INT_MIN) {
+    float v = bilinear_at(img, bps, W, H, kx, s_a[threadIdx.x], ky, s_a[32 + threadIdx.y]);
     r = a.mode == 0 ? 1.0f - v : (a.threshold <= v ? 1.0f : 0.0f);
   }
   out[(size_t)y * w + x] = r;
