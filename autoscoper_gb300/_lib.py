@@ -8,6 +8,7 @@ import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SO = os.environ.get("ASC_LIB_PATH") or os.path.join(HERE, "libautoscoper_gb300.so")
+TUNING = os.path.join(HERE, "tuning.txt")
 
 vp = C.c_void_p
 i32 = C.c_int
@@ -42,6 +43,10 @@ class ViewDesc(C.Structure):
     _fields_ = [("frame", f64 * 12), ("viewport", f64 * 4), ("image_plane", f64 * 12), ("radiograph", vp),
                 ("background", vp), ("bg_threshold", f32), ("n_drr_filters", i32), ("n_rad_filters", i32),
                 ("drr_filters", FilterDesc * 8), ("rad_filters", FilterDesc * 8)]
+
+
+class LaunchConfig(C.Structure):
+    _fields_ = [("ray_blocks_per_sm", i32), ("view_blocks_per_sm", i32), ("ray_shape", i32)]
 
 
 class BoneDesc(C.Structure):
@@ -100,6 +105,12 @@ SIGNATURES = {
     "asc_hdist_host": (i32, [vp, vp, vp, C.c_uint, i32, P(f64), vp]),
     "asc_engine_create": (i32, [i32, P(ViewDesc), i32, P(BoneDesc), i32, i32, i32, i32, i32, P(vp)]),
     "asc_engine_destroy": (i32, [vp]),
+    "asc_engine_set_launch": (i32, [vp, P(LaunchConfig)]),
+    "asc_engine_get_launch": (i32, [vp, P(LaunchConfig), P(i32)]),
+    "asc_engine_workload_class": (i32, [vp, P(i32)]),
+    "asc_tuning_load": (i32, [C.c_char_p]),
+    "asc_engine_set_view": (i32, [vp, i32, P(ViewDesc), i32, i32]),
+    "asc_engine_set_bone": (i32, [vp, i32, P(BoneDesc), i32, P(i32)]),
     "asc_engine_set_base_pose": (i32, [vp, i32, P(f64)]),
     "asc_engine_set_radiograph": (i32, [vp, i32, vp]),
     "asc_engine_set_visible": (i32, [vp, i32, i32]),
@@ -161,6 +172,9 @@ def load(path: str = SO):
             fn.restype = res
             fn.argtypes = args
         _LIB = lib
+        # the autotuner's launch shapes per workload class, for the engines created from here on
+        if os.path.exists(TUNING):
+            check("asc_tuning_load", lib.asc_tuning_load(TUNING.encode()))
     return _LIB
 
 

@@ -225,6 +225,32 @@ def _filters(lst, arr):
     return n
 
 
+def fill_view_desc(d, v: S.View, radiograph: "DeviceImage", background: "DeviceImage" = None):
+    """An asc_view_desc of a scene view (camera, radiograph, background and
+    the two filter lists)."""
+    d.frame[:] = list(v.camera.frame)
+    d.viewport[:] = list(v.camera.viewport)
+    d.image_plane[:] = list(v.camera.image_plane)
+    d.radiograph = radiograph.handle
+    d.background = background.handle if background else None
+    d.bg_threshold = v.bg_threshold
+    d.n_drr_filters = _filters(v.drr_filters, d.drr_filters)
+    d.n_rad_filters = _filters(v.rad_filters, d.rad_filters)
+    return d
+
+
+def fill_bone_desc(d, volume: "DeviceVolume", pivot, base_pose, rays):
+    """An asc_bone_desc: the volume, its pivot, the base pose (rounded to
+    float as the key curves hold it) and the RayCaster settings of each of
+    its views in order (rays: list of S.RayParams)."""
+    d.volume = volume.handle
+    d.pivot[:] = list(pivot)
+    d.base_pose[:] = [float(x) for x in np.asarray(base_pose, np.float32)]
+    for j, rp in enumerate(rays):
+        d.step[j], d.intensity[j], d.cutoff[j] = rp.step, rp.intensity, rp.cutoff
+    return d
+
+
 class Engine:
     """A scene resident on the device (asc_engine_create) that scores
     (bone, manipulator) candidates with Tracker::minimizationFunc semantics."""
@@ -238,24 +264,11 @@ class Engine:
         nv, nb = len(scene.views), len(scene.volumes)
         views = (L.ViewDesc * nv)()
         for i, v in enumerate(scene.views):
-            d = views[i]
-            d.frame[:] = list(v.camera.frame)
-            d.viewport[:] = list(v.camera.viewport)
-            d.image_plane[:] = list(v.camera.image_plane)
-            d.radiograph = self.rads[i].handle
-            d.background = self.bgs[i].handle if self.bgs[i] else None
-            d.bg_threshold = v.bg_threshold
-            d.n_drr_filters = _filters(v.drr_filters, d.drr_filters)
-            d.n_rad_filters = _filters(v.rad_filters, d.rad_filters)
+            fill_view_desc(views[i], v, self.rads[i], self.bgs[i])
         bones = (L.BoneDesc * nb)()
         for b in range(nb):
-            d = bones[b]
-            d.volume = self.vols[b].handle
-            d.pivot[:] = list(scene.pivots[b])
-            d.base_pose[:] = [float(x) for x in np.asarray(scene.poses[b], np.float32)]
-            for v in range(nv):
-                rp = scene.ray[v][b]
-                d.step[v], d.intensity[v], d.cutoff[v] = rp.step, rp.intensity, rp.cutoff
+            fill_bone_desc(bones[b], self.vols[b], scene.pivots[b], scene.poses[b],
+                           [scene.ray[v][b] for v in range(min(nv, 4))])
         h = C.c_void_p()
         L.call("asc_engine_create", nv, views, nb, bones, scene.render_width, scene.render_height, max_items,
                coverage, scene.cf_model, C.byref(h))

@@ -16,12 +16,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
-# ASC_BUILD_TAG / ASC_NVCC_DEFS build a tagged variant next to the default
-# library (used to compare kernel variants); the default build sets neither.
-TAG = os.environ.get("ASC_BUILD_TAG", "")
-OUT = os.path.join(HERE, f"libautoscoper_gb300{'_' + TAG if TAG else ''}.so")
-BUILD = os.path.join(HERE, f"_build{'_' + TAG if TAG else ''}")
-DEFS = os.environ.get("ASC_NVCC_DEFS", "").split()
+OUT = os.path.join(HERE, "libautoscoper_gb300.so")
+BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
          "--expt-relaxed-constexpr",
@@ -51,7 +47,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         o = os.path.join(BUILD, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc(), *ARCH, *FLAGS, *DEFS, "-c", s, "-o", o])
+            jobs.append([nvcc(), *ARCH, *FLAGS, "-c", s, "-o", o])
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         for cmd, r in zip(jobs, ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs)):
             if verbose or r.returncode:

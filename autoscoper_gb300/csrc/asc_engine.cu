@@ -20,7 +20,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "asc_internal.cuh"
@@ -33,8 +36,9 @@ using namespace asc;
 
 namespace {
 
-constexpr int MAX_VIEWS = 4;
-constexpr int MAX_BONES = 16;
+constexpr int MAX_VIEWS = 16;  // views of an engine (a serving engine holds several jobs' views)
+constexpr int MAX_SLOTS = 4;   // views one bone is scored in (the public bone desc's per-view settings)
+constexpr int MAX_BONES = 64;
 constexpr int MAX_FILTERS = 8;
 #ifndef ASC_VT
 #define ASC_VT 48
@@ -57,6 +61,8 @@ struct FilterDev {
 struct ViewDev {
   double cam[12], cam_inv[12], ip[12], cvp[4];
   float ipf[4];
+  int rw, rh;  // render size of this view's trial (Trial::render_width/height)
+  int E;       // k_view region edge: VT + 2 x the larger chain halo
   const void* rad;
   int rad_w, rad_h, rad_bps;
   const float* bg;
@@ -70,13 +76,18 @@ struct BoneDev {
   DevVolume vol;
   float inv_scale[3], inv_trans[3];
   double pivot[12], pivot_inv[12], base[6];
-  float step[MAX_VIEWS], scale[MAX_VIEWS], cutoff_raw[MAX_VIEWS];
-  const uint8_t* occ[MAX_VIEWS];  // empty-cell grids per view's cutoff
+  // per slot: the bone is scored in views view_of[0 .. n_slots), with that
+  // view's RayCaster settings and its empty-cell grid
+  float step[MAX_SLOTS], scale[MAX_SLOTS], cutoff_raw[MAX_SLOTS];
+  const uint8_t* occ[MAX_SLOTS];
+  int view_of[MAX_SLOTS];
+  int n_slots;
   int visible;                    // RayCaster::setVisible: a hidden volume renders zeros
 };
 
 struct SceneDev {
-  int n_views, n_bones, rw, rh, coverage, E;
+  int n_views, n_bones, rw, rh, coverage, E;  // rw, rh, E: the largest of the views'
+  int slots;     // (item, slot) entries per item: the most views a bone is scored in
   int cf_model;  // 0: 1 - NCC per view; 1: SAD ("hdist") per view
   ViewDev views[MAX_VIEWS];
   BoneDev bones[MAX_BONES];
@@ -87,6 +98,7 @@ struct IV {
   float vp[4];
   float sx[2], sy[2];  // vp[2] / w and vp[3] / h as double-floats
   int w, h, ok, bone;
+  int view, slot;  // the engine view and the bone's slot of this (item, view)
   int rtx, rty, ftx, fty;
   int err;        // the crop exceeded the render size (the reference throws)
   long long pix;  // offset of this crop in the DRR buffer
@@ -130,7 +142,7 @@ __device__ __forceinline__ int find_iv(const int* off, int n, int tile)
 __device__ void finish_item(const SceneDev* sc, const Bufs& b, int item, double* cost)
 {
   double tot = 0;
-  for (int v = 0; v < sc->n_views; ++v) tot += b.vcost[item * sc->n_views + v];
+  for (int j = 0; j < sc->slots; ++j) tot += b.vcost[item * sc->slots + j];
   cost[item] = tot < 0 ? 9999.0 : tot;  // Tracker.cpp:823-825
 }
 
@@ -140,14 +152,24 @@ __device__ void finish_item(const SceneDev* sc, const Bufs& b, int item, double*
 __device__ void setup_iv(const SceneDev* __restrict__ sc, int k, const int* __restrict__ bone_in,
                          const double* __restrict__ manip, const Bufs& b)
 {
-  const int nv = sc->n_views;
-  const int item = k / nv, v = k % nv;
+  const int ns = sc->slots;
+  const int item = k / ns, j = k % ns;
   IV r;
   memset(&r, 0, sizeof r);
   int bi = bone_in[item];
   if (bi < 0 || bi >= sc->n_bones) bi = 0;
   r.bone = bi;
+  r.slot = j;
   const BoneDev& B = sc->bones[bi];
+  if (j >= B.n_slots) {  // a slot this bone has no view in: adds nothing to the cost
+    r.view = -1;
+    b.iv[k] = r;
+    b.vcost[k] = 0.0;
+    b.ivt[k] = 0;
+    return;
+  }
+  const int v = B.view_of[j];
+  r.view = v;
   const ViewDev& V = sc->views[v];
   // minimizationFunc: pose . V^-1 . manip . V, then the xyzypr round trip
   double base[12], man[12], t1[12], t2[12], xyz[6];
@@ -168,9 +190,9 @@ __device__ void setup_iv(const SceneDev* __restrict__ sc, int k, const int* __re
   if (!calculate_viewport(mv, V.cam, V.ip, B.inv_scale, B.inv_trans, vp)) {
     vc = 9999.0;  // Tracker.cpp:614-617
   } else {
-    double fw = vp[2] * sc->rw / V.cvp[2], fh = vp[3] * sc->rh / V.cvp[3];
+    double fw = vp[2] * V.rw / V.cvp[2], fh = vp[3] * V.rh / V.cvp[3];
     unsigned w = fw > 0 ? (unsigned)fw : 0u, h = fh > 0 ? (unsigned)fh : 0u;
-    if (w > (unsigned)sc->rw || h > (unsigned)sc->rh) {
+    if (w > (unsigned)V.rw || h > (unsigned)V.rh) {
       r.err = 1;  // the reference throws (Tracker.cpp:625-629)
       w = 0;
       h = 0;
@@ -206,7 +228,7 @@ __global__ void __launch_bounds__(128) k_setup_iv(const SceneDev* __restrict__ s
                                                   Bufs b)
 {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n_items * sc->n_views) setup_iv(sc, k, bone_in, manip, b);
+  if (k < n_items * sc->slots) setup_iv(sc, k, bone_in, manip, b);
 }
 
 // The layout of a batch after k_setup_iv: prefix sums of the tile counts and
@@ -216,7 +238,7 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
                                                  double* __restrict__ cost)
 {
   __shared__ int s_err;
-  const int nv = sc->n_views, n_iv = n_items * nv;
+  const int nv = sc->slots, n_iv = n_items * nv;
   const int per = (n_iv + blockDim.x - 1) / blockDim.x;
   const int i0 = threadIdx.x * per, i1 = min(i0 + per, n_iv);
   if (threadIdx.x == 0) s_err = 0;
@@ -331,7 +353,10 @@ __device__ __forceinline__ void march_segments(const DevVolume& V, const float4 
   }
 }
 
-__global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev* __restrict__ sc, Bufs b, int skip)
+// shape: log2 of the width of the ray block each warp takes in a 16 x 16
+// tile (2: 4 x 8, 3: 8 x 4, 4: 16 x 2), the autotuner's choice.
+__global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev* __restrict__ sc, Bufs b, int skip,
+                                                                 int shape)
 {
   static_assert(REBASE == 64 && NRAY * NBW <= 2048, "segment fields: 11-bit slot, 6-bit offsets");
   __shared__ float4 s_rec[3][NRAY];      // per ray: X, Y, Z, dX, dY, dZ as double-floats
@@ -343,7 +368,6 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
   __shared__ int s_tile, s_nseg, s_grab, s_k;
   const unsigned FULL = 0xffffffffu;
   const int tid = threadIdx.x, lane = tid & 31;
-  const int nv = sc->n_views;
   unsigned long long marched = 0, slots = 0, sampled = 0;
   for (;;) {
     if (tid == 0) {
@@ -357,16 +381,19 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
     const int k = s_k;
     const IV& r = b.iv[k];
     const int t = tile - b.roff[k];
-    // each warp takes an 8 x 4 block of the 16 x 16 tile (coherent walks)
-    const int x = (t % r.rtx) * RTX + (tid & 7) + 8 * ((tid >> 5) & 1),
-              y = (t / r.rtx) * RTY + ((tid >> 3) & 3) + 4 * (tid >> 6);
+    // each warp takes a (1 << shape) x (32 >> shape) block of the 16 x 16
+    // tile (coherent walks)
+    const int wsh = shape, wpr = 4 - shape;  // log2 of the block width, of the blocks per tile row
+    const int wrp = tid >> 5;
+    const int x = (t % r.rtx) * RTX + ((wrp & ((1 << wpr) - 1)) << wsh) + (lane & ((1 << wsh) - 1)),
+              y = (t / r.rtx) * RTY + ((wrp >> wpr) << (5 - wsh)) + (lane >> wsh);
     const bool valid = x < r.w && y < r.h;
     const BoneDev& B = sc->bones[r.bone];
-    const int v = k % nv;
-    const float cut = B.cutoff_raw[v];
-    const uint8_t* occ = skip ? B.occ[v] : nullptr;
+    const int j = r.slot;
+    const float cut = B.cutoff_raw[j];
+    const uint8_t* occ = skip ? B.occ[j] : nullptr;
     RaySetup rs{};
-    const bool hit = valid && ray_setup(r.m, r.vp, x, y, df{r.sx[0], r.sx[1]}, df{r.sy[0], r.sy[1]}, B.step[v],
+    const bool hit = valid && ray_setup(r.m, r.vp, x, y, df{r.sx[0], r.sx[1]}, df{r.sy[0], r.sy[1]}, B.step[j],
                                         B.vol.nx, B.vol.ny, B.vol.nz, rs);
     // trilinear samples of the reference's march (the work figure of the
     // roofline), counted per warp and added to the global count once at the end
@@ -442,7 +469,7 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
       for (int i = 0; i < n; ++i) add_block(total, s_part[tid * NBW + i]);
       if (!__syncthreads_or(!done)) break;
     }
-    if (valid) b.drr[r.pix + (long long)y * r.w + x] = fminf(fmaxf((total.h + total.l) * B.scale[v], 0.f), 1.f);
+    if (valid) b.drr[r.pix + (long long)y * r.w + x] = fminf(fmaxf((total.h + total.l) * B.scale[j], 0.f), 1.f);
   }
   if (lane == 0 && sampled) atomicAdd(&b.C->samples, sampled);
   if (lane == 0 && slots) {
@@ -759,17 +786,8 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
   __shared__ float red[8 * 6 * 2];
   __shared__ double ds[6], dc[3];
   __shared__ float wsh[32];
-  const int E = sc->E, eh = (E - VT) / 2;
-  float* bufs[3] = {smem, smem + E * E, smem + 2 * E * E};
-  float* fdrr = smem + 3 * E * E;        // VT x VT final DRR, then f = DRR * mask
   Moments* msh = (Moments*)smem;          // reused by the merge
-  // per region column / row: the radiograph texel pair and weight of the
-  // film-plane mapping (image_axis; kNoTexel where the pixel maps outside)
-  int* tcx = (int*)(smem + view_tail_floats(E));
-  float* tax = (float*)(tcx + E);
-  int* tcy = (int*)(tax + E);
-  float* tay = (float*)(tcy + E);
-  const int nv = sc->n_views;
+  const int ns = sc->slots;
   for (;;) {
     if (threadIdx.x == 0) {
       const int tl = atomicAdd(&b.C->fnext, 1);
@@ -783,8 +801,17 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
     const IV& r = b.iv[k];
     const int t = tile - b.foff[k];
     const int tx0 = (t % r.ftx) * VT, ty0 = (t / r.ftx) * VT;
-    const int v = k % nv;
-    const ViewDev& V = sc->views[v];
+    const ViewDev& V = sc->views[r.view];
+    // this view's region edge E (its chain's halo) lays out the shared memory
+    const int E = V.E, eh = (E - VT) / 2;
+    float* bufs[3] = {smem, smem + E * E, smem + 2 * E * E};
+    float* fdrr = smem + 3 * E * E;  // VT x VT final DRR, then f = DRR * mask
+    // per region column / row: the radiograph texel pair and weight of the
+    // film-plane mapping (image_axis; kNoTexel where the pixel maps outside)
+    int* tcx = (int*)(smem + view_tail_floats(E));
+    float* tax = (float*)(tcx + E);
+    int* tcy = (int*)(tax + E);
+    float* tay = (float*)(tcy + E);
     const int rx0 = tx0 - eh, ry0 = ty0 - eh;
     const Region g{rx0, ry0, E, r.w, r.h, rx0 >= 0 && ry0 >= 0 && rx0 + E <= r.w && ry0 + E <= r.h};
     const float* drr = b.drr + r.pix;
@@ -936,12 +963,12 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
       double vc = 1.0 - moments_ncc(msh[0]);
       b.vcost[k] = vc;
       __threadfence();
-      const int item = k / nv;
-      if (atomicAdd(&b.itt[item], 1u) == (unsigned)nv - 1) {
+      const int item = k / ns;
+      if (atomicAdd(&b.itt[item], 1u) == (unsigned)ns - 1) {
         __threadfence();
         finish_item(sc, b, item, cost);
         if (view_cost_out)
-          for (int j = 0; j < nv; ++j) view_cost_out[item * nv + j] = b.vcost[item * nv + j];
+          for (int j = 0; j < ns; ++j) view_cost_out[item * ns + j] = b.vcost[item * ns + j];
       }
     }
     __syncthreads();
@@ -960,7 +987,7 @@ __global__ void __launch_bounds__(256) k_sad(const SceneDev* __restrict__ sc, Bu
   __shared__ float red[8];
   __shared__ double dred[8];
   __shared__ bool s_last;
-  const int nv = sc->n_views, ftiles = b.C->ftiles;
+  const int nv = sc->slots, ftiles = b.C->ftiles;
   for (int tile = blockIdx.x; tile < ftiles; tile += gridDim.x) {
     const int k = find_iv(b.foff, b.C->n_iv, tile);
     const IV& r = b.iv[k];
@@ -1142,7 +1169,16 @@ struct asc_engine_s {
   Bufs b{};
   size_t smem = 0;
   int sms = 152;
-  int view_blocks = 1;  // resident k_view blocks per SM
+  int view_blocks = 1;  // resident k_view blocks per SM (the occupancy limit)
+  // launch shapes (asc_engine_set_launch): the defaults, or the tuning
+  // table's entry for this engine's workload class
+  asc_launch_config launch{ASC_RAY_MINBLOCKS, 0, 3};
+  // k_view blocks per SM: the configured count, at most the occupancy limit
+  int view_grid() const
+  {
+    const int want = launch.view_blocks_per_sm;
+    return want > 0 ? std::min(want, view_blocks) : view_blocks;
+  }
   bool prof = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   // device PSO: swarm state, the captured iteration and a private stream
@@ -1162,9 +1198,16 @@ struct asc_engine_s {
   float *p_drr = nullptr, *p_rad = nullptr, *p_mask = nullptr, *p_bg = nullptr, *p_tmp = nullptr, *p_bgr = nullptr;
   double* p_res = nullptr;
   std::vector<void*> allocs;
+  // empty-cell grids of bones replaced by asc_engine_set_bone, per (bone,
+  // slot), with their capacity in bytes
+  uint8_t* occ_own[MAX_BONES][MAX_SLOTS] = {};
+  size_t occ_cap[MAX_BONES][MAX_SLOTS] = {};
   ~asc_engine_s()
   {
     for (void* p : allocs) cudaFree(p);
+    for (auto& row : occ_own)
+      for (uint8_t* p : row)
+        if (p) cudaFree(p);
     for (cudaEvent_t x : ev)
       if (x) cudaEventDestroy(x);
     if (pso_exec) cudaGraphExecDestroy(pso_exec);
@@ -1239,10 +1282,18 @@ static int fill_view(ViewDev& d, const asc_view_desc& v)
   n = prep_filters(v.rad_filters, v.n_rad_filters, d.frad, &d.h_rad);
   if (n < 0) return n;
   d.n_rad = n;
+  d.E = VT + 2 * std::max(d.h_drr, d.h_rad);
+  // three E x E stage buffers, the tile and the mapping tables must fit one
+  // block's shared memory (227 KB less the static arrays)
+  if (view_smem_floats(d.E) * sizeof(float) > 224 * 1024) return ASC_ERR_RANGE;
   return ASC_OK;
 }
 
 static void set_base(BoneDev& B, const double* xyzypr) { memcpy(B.base, xyzypr, sizeof B.base); }
+
+namespace {
+void apply_tuning(asc_engine_s* e);  // the tuning table's launch shapes, below
+}
 
 ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bones, const asc_bone_desc* bones,
                               int rw, int rh, int max_items, int coverage, int cf_model, asc_engine* out)
@@ -1269,21 +1320,17 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
   S.rh = rh;
   S.coverage = coverage;
   S.cf_model = cf_model;
-  int hmax = 0;
+  S.slots = std::min(n_views, MAX_SLOTS);
+  S.E = 0;
   for (int v = 0; v < n_views; ++v) {
     int rc = fill_view(S.views[v], views[v]);
     if (rc) {
       delete e;
       return rc;
     }
-    hmax = std::max(hmax, std::max(S.views[v].h_drr, S.views[v].h_rad));
-  }
-  S.E = VT + 2 * hmax;
-  // three E x E stage buffers and the final tile must fit one block's shared
-  // memory (227 KB less the static arrays)
-  if (view_smem_floats(S.E) * sizeof(float) > 224 * 1024) {
-    delete e;
-    return ASC_ERR_RANGE;
+    S.views[v].rw = rw;
+    S.views[v].rh = rh;
+    S.E = std::max(S.E, S.views[v].E);
   }
   for (int i = 0; i < n_bones; ++i) {
     auto* vh = (asc_volume_host*)bones[i].volume;
@@ -1299,23 +1346,25 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
     frame_inverse(B.pivot, B.pivot_inv);
     set_base(B, bones[i].base_pose);
     B.visible = 1;
-    for (int v = 0; v < n_views; ++v) {
-      B.step[v] = bones[i].step[v];
-      B.scale[v] = bones[i].step[v] * vh->dev.norm / bones[i].intensity[v];
-      B.cutoff_raw[v] = bones[i].cutoff[v] / vh->dev.norm;
+    B.n_slots = S.slots;  // bone i is scored in views 0 .. slots - 1
+    for (int j = 0; j < S.slots; ++j) {
+      B.view_of[j] = j;
+      B.step[j] = bones[i].step[j];
+      B.scale[j] = bones[i].step[j] * vh->dev.norm / bones[i].intensity[j];
+      B.cutoff_raw[j] = bones[i].cutoff[j] / vh->dev.norm;
       uint8_t* occ = nullptr;
       if (e->alloc(occ, occ_grid_bytes(occupancy_cells(vh->dev)))) {
         delete e;
         return ASC_ERR_NOMEM;
       }
-      build_occupancy(vh->dev, B.cutoff_raw[v], occ, cs);
-      B.occ[v] = occ;
+      build_occupancy(vh->dev, B.cutoff_raw[j], occ, cs);
+      B.occ[j] = occ;
     }
   }
   e->max_items = max_items;
   e->n_views = n_views;
   e->n_bones = n_bones;
-  size_t n_iv = (size_t)max_items * n_views;
+  size_t n_iv = (size_t)max_items * S.slots;
   size_t tiles = (size_t)((rw + VT - 1) / VT) * ((rh + VT - 1) / VT);
   cudaError_t err = e->alloc(e->dev, 1);
   if (!err) err = e->alloc(e->b.iv, n_iv);
@@ -1368,6 +1417,7 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
     return cuda_status(err);
   }
   e->view_blocks = std::max(e->view_blocks, 1);
+  apply_tuning(e);
   *out = e;
   return ASC_OK;
 }
@@ -1415,20 +1465,200 @@ ASC_API int asc_engine_set_radiograph(asc_engine e, int view, asc_image rad)
   return ASC_OK;
 }
 
+ASC_API int asc_engine_set_view(asc_engine e, int view, const asc_view_desc* desc, int rw, int rh)
+{
+  if (!e || !desc || view < 0 || view >= e->n_views || rw < 1 || rh < 1 || rw > e->host.rw || rh > e->host.rh)
+    return ASC_ERR_ARG;
+  ViewDev d;
+  memset(&d, 0, sizeof d);
+  int rc = fill_view(d, *desc);
+  if (rc) return rc;
+  d.rw = rw;
+  d.rh = rh;
+  Gate g(device_gate());
+  const size_t need = view_smem_floats(d.E) * sizeof(float);
+  if (need > e->smem) {  // a wider filter chain than the engine's views had so far
+    int blocks = 0;
+    ASC_CUDA(cudaFuncSetAttribute(k_view, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    ASC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_view, VNT, need));
+    e->smem = need;
+    e->view_blocks = std::max(blocks, 1);
+    e->host.E = std::max(e->host.E, d.E);
+    if (e->pso_exec) {  // its k_view node holds the old launch shape
+      cudaGraphExecDestroy(e->pso_exec);
+      e->pso_exec = nullptr;
+    }
+  }
+  e->host.views[view] = d;
+  e->vdesc[view] = *desc;
+  ASC_CUDA(cudaMemcpy(&e->dev->views[view], &d, sizeof d, cudaMemcpyHostToDevice));
+  return ASC_OK;
+}
+
+ASC_API int asc_engine_set_bone(asc_engine e, int bone, const asc_bone_desc* desc, int n_views, const int* views)
+{
+  if (!e || !desc || !desc->volume || bone < 0 || bone >= e->n_bones || n_views < 1 || n_views > e->host.slots ||
+      !views)
+    return ASC_ERR_ARG;
+  for (int j = 0; j < n_views; ++j)
+    if (views[j] < 0 || views[j] >= e->n_views) return ASC_ERR_ARG;
+  auto* vh = (asc_volume_host*)desc->volume;
+  BoneDev B = e->host.bones[bone];
+  B.vol = vh->dev;
+  memcpy(B.inv_scale, vh->inv_scale, sizeof B.inv_scale);
+  memcpy(B.inv_trans, vh->inv_trans, sizeof B.inv_trans);
+  memcpy(B.pivot, desc->pivot, sizeof B.pivot);
+  frame_inverse(B.pivot, B.pivot_inv);
+  set_base(B, desc->base_pose);
+  B.visible = 1;
+  B.n_slots = n_views;
+  Gate g(device_gate());
+  const size_t grid = occ_grid_bytes(occupancy_cells(vh->dev));
+  for (int j = 0; j < n_views; ++j) {
+    B.view_of[j] = views[j];
+    B.step[j] = desc->step[j];
+    B.scale[j] = desc->step[j] * vh->dev.norm / desc->intensity[j];
+    B.cutoff_raw[j] = desc->cutoff[j] / vh->dev.norm;
+    uint8_t*& occ = e->occ_own[bone][j];
+    if (e->occ_cap[bone][j] < grid) {
+      if (occ) cudaFree(occ);
+      occ = nullptr;
+      e->occ_cap[bone][j] = 0;
+      ASC_CUDA(cudaMalloc(&occ, grid));
+      e->occ_cap[bone][j] = grid;
+    }
+    build_occupancy(vh->dev, B.cutoff_raw[j], occ, nullptr);
+    B.occ[j] = occ;
+  }
+  ASC_CUDA(cudaStreamSynchronize(nullptr));
+  e->host.bones[bone] = B;
+  e->bdesc[bone] = *desc;
+  ASC_CUDA(cudaMemcpy(&e->dev->bones[bone], &B, sizeof B, cudaMemcpyHostToDevice));
+  return ASC_OK;
+}
+
+// ---- the tuning table: launch shapes per workload class, written by the
+// project's autotuner (autoscoper_gb300/tune.py) and read at engine creation.
+// A class is (ceil log2 of the render pixels, ceil log2 of the largest
+// volume's voxels, views); a line of the table holds
+//   rpx vox views ray_blocks_per_sm view_blocks_per_sm ray_shape
+// ('#' starts a comment).  An engine takes the entry of its render size and
+// view count with the nearest volume class; without one it keeps the defaults.
+namespace {
+struct TuneEntry {
+  int rpx, vox, views;
+  asc_launch_config cfg;
+};
+std::mutex g_tune_mu;
+std::vector<TuneEntry> g_tune;
+
+int ceil_log2(double x)
+{
+  int k = 0;
+  while ((double)(1ull << k) < x && k < 62) ++k;
+  return k;
+}
+
+void workload_class(const asc_engine_s* e, int out[3])
+{
+  double vox = 0;
+  for (int b = 0; b < e->n_bones; ++b) {
+    const DevVolume& V = e->host.bones[b].vol;
+    vox = std::max(vox, (double)V.nx * V.ny * V.nz);
+  }
+  out[0] = ceil_log2((double)e->host.rw * e->host.rh);
+  out[1] = ceil_log2(vox);
+  out[2] = e->n_views;
+}
+
+void apply_tuning(asc_engine_s* e)
+{
+  int c[3];
+  workload_class(e, c);
+  std::lock_guard<std::mutex> l(g_tune_mu);
+  const TuneEntry* best = nullptr;
+  for (const TuneEntry& t : g_tune)
+    if (t.rpx == c[0] && t.views == c[2] && (!best || std::abs(t.vox - c[1]) < std::abs(best->vox - c[1])))
+      best = &t;
+  if (best) e->launch = best->cfg;
+}
+}  // namespace
+
+ASC_API int asc_tuning_load(const char* path)
+{
+  if (!path) return ASC_ERR_ARG;
+  FILE* f = fopen(path, "r");
+  if (!f) return ASC_ERR_ARG;
+  std::vector<TuneEntry> t;
+  char line[512];
+  int rc = ASC_OK;
+  while (fgets(line, sizeof line, f)) {
+    char* hash = strchr(line, '#');
+    if (hash) *hash = 0;
+    TuneEntry x;
+    int n = sscanf(line, "%d %d %d %d %d %d", &x.rpx, &x.vox, &x.views, &x.cfg.ray_blocks_per_sm,
+                   &x.cfg.view_blocks_per_sm, &x.cfg.ray_shape);
+    if (n <= 0) continue;  // blank or comment
+    if (n != 6 || x.cfg.ray_blocks_per_sm < 1 || x.cfg.ray_blocks_per_sm > ASC_RAY_MINBLOCKS ||
+        x.cfg.view_blocks_per_sm < 0 || x.cfg.ray_shape < 2 || x.cfg.ray_shape > 4) {
+      rc = ASC_ERR_ARG;
+      break;
+    }
+    t.push_back(x);
+  }
+  fclose(f);
+  if (rc) {
+    set_error_message("asc_tuning_load: a line is not 'rpx vox views ray_blocks view_blocks ray_shape'");
+    return rc;
+  }
+  std::lock_guard<std::mutex> l(g_tune_mu);
+  g_tune = t;
+  return ASC_OK;
+}
+
+ASC_API int asc_engine_workload_class(asc_engine e, int out[3])
+{
+  if (!e || !out) return ASC_ERR_ARG;
+  workload_class(e, out);
+  return ASC_OK;
+}
+
+ASC_API int asc_engine_set_launch(asc_engine e, const asc_launch_config* cfg)
+{
+  if (!e || !cfg || cfg->ray_blocks_per_sm < 1 || cfg->ray_blocks_per_sm > ASC_RAY_MINBLOCKS ||
+      cfg->view_blocks_per_sm < 0 || cfg->ray_shape < 2 || cfg->ray_shape > 4)
+    return ASC_ERR_ARG;
+  Gate g(device_gate());
+  e->launch = *cfg;
+  if (e->pso_exec) {  // the captured iteration holds the old launch shapes
+    cudaGraphExecDestroy(e->pso_exec);
+    e->pso_exec = nullptr;
+  }
+  return ASC_OK;
+}
+
+ASC_API int asc_engine_get_launch(asc_engine e, asc_launch_config* cfg, int* view_blocks_max)
+{
+  if (!e || !cfg) return ASC_ERR_ARG;
+  *cfg = e->launch;
+  if (view_blocks_max) *view_blocks_max = e->view_blocks;
+  return ASC_OK;
+}
+
 static int engine_launch(asc_engine e, int n, const int* bone, const double* manip, double* cost, double* vcost,
                          cudaStream_t s, bool capturing = false)
 {
   const bool prof = e->prof && !capturing;
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[0], s));
-  k_setup_iv<<<(n * e->n_views + 127) / 128, 128, 0, s>>>(e->dev, n, bone, manip, e->b);
+  k_setup_iv<<<(n * e->host.slots + 127) / 128, 128, 0, s>>>(e->dev, n, bone, manip, e->b);
   k_setup<<<1, 1024, 0, s>>>(e->dev, n, e->b, cost);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[1], s));
-  k_ray<<<e->sms * ASC_RAY_MINBLOCKS, NRAY, 0, s>>>(e->dev, e->b, g_empty_skip);
+  k_ray<<<e->sms * e->launch.ray_blocks_per_sm, NRAY, 0, s>>>(e->dev, e->b, g_empty_skip, e->launch.ray_shape);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[2], s));
-  k_view<<<e->sms * e->view_blocks, VNT, e->smem, s>>>(e->dev, e->b, cost, vcost);
+  k_view<<<e->sms * e->view_grid(), VNT, e->smem, s>>>(e->dev, e->b, cost, vcost);
   if (e->host.cf_model) k_sad<<<e->sms * 8, 256, 0, s>>>(e->dev, e->b, cost, vcost);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[3], s));
-  if (vcost) k_copy_vcost<<<8, 256, 0, s>>>(e->b.vcost, vcost, n * e->n_views);
+  if (vcost) k_copy_vcost<<<8, 256, 0, s>>>(e->b.vcost, vcost, n * e->host.slots);
   ASC_LAUNCH_CHECK();
   return ASC_OK;
 }
@@ -1487,7 +1717,7 @@ ASC_API int asc_engine_eval_host(asc_engine e, int n, const int* bone, const dou
   if (rc) return rc;
   ASC_CUDA(cudaMemcpyAsync(cost, e->d_cost, n * sizeof(double), cudaMemcpyDeviceToHost, s));
   if (vcost)
-    ASC_CUDA(cudaMemcpyAsync(vcost, e->d_vcost, (size_t)n * e->n_views * sizeof(double), cudaMemcpyDeviceToHost, s));
+    ASC_CUDA(cudaMemcpyAsync(vcost, e->d_vcost, (size_t)n * e->host.slots * sizeof(double), cudaMemcpyDeviceToHost, s));
   Counters C;
   ASC_CUDA(cudaMemcpyAsync(&C, e->b.C, sizeof C, cudaMemcpyDeviceToHost, s));
   ASC_CUDA(cudaStreamSynchronize(s));
@@ -1637,6 +1867,23 @@ static void view_matrix(const ViewDev& V, const BoneDev& B, const double* xyzypr
   fold_matrix(imv16, B.inv_scale, B.inv_trans, m);
 }
 
+// Whether every bone is scored in every view, slot j being view j (the
+// layout asc_engine_create makes for up to MAX_SLOTS views).  The plain
+// per-pose path and the image exports read the bones' per-view settings by
+// view and need it; engines whose bones asc_engine_set_bone moved to other
+// views serve batched evaluations only.
+static bool identity_slots(const asc_engine_s* e)
+{
+  if (e->host.slots != e->n_views) return false;
+  for (int b = 0; b < e->n_bones; ++b) {
+    const BoneDev& B = e->host.bones[b];
+    if (B.n_slots != e->n_views) return false;
+    for (int j = 0; j < B.n_slots; ++j)
+      if (B.view_of[j] != j) return false;
+  }
+  return true;
+}
+
 // RayCaster::render (RayCaster.cpp:123-143) of one bone into `out`: zeros
 // for a hidden volume.
 static int render_bone(const BoneDev& B, const asc_bone_desc& BD, int v, const float* m, const float* vpf,
@@ -1654,6 +1901,7 @@ ASC_API int asc_engine_eval_plain(asc_engine e, int n, const int* bone, const do
                                   double* view_cost, void* stream)
 {
   if (!e || !bone || !manip || !cost || n < 1) return ASC_ERR_ARG;
+  if (!identity_slots(e)) return ASC_ERR_STATE;
   cudaStream_t s = S(stream);
   const SceneDev& S_ = e->host;
   const int nv = e->n_views;
@@ -1962,6 +2210,7 @@ ASC_API int asc_engine_render_drr(asc_engine e, int view, const double* poses, c
                                   void* stream)
 {
   if (!e || !poses || !out || view < 0 || view >= e->n_views) return ASC_ERR_ARG;
+  if (!identity_slots(e)) return ASC_ERR_STATE;
   cudaStream_t s = S(stream);
   const ViewDev& V = e->host.views[view];
   const asc_view_desc& VD = e->vdesc[view];
@@ -1997,6 +2246,7 @@ ASC_API int asc_engine_image_data(asc_engine e, int view, int bone, const double
 {
   if (!e || !pose || !rad || !drr || !mask || view < 0 || view >= e->n_views || bone < 0 || bone >= e->n_bones)
     return ASC_ERR_ARG;
+  if (!identity_slots(e)) return ASC_ERR_STATE;
   cudaStream_t s = S(stream);
   const ViewDev& V = e->host.views[view];
   const asc_view_desc& VD = e->vdesc[view];

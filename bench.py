@@ -112,6 +112,27 @@ def profile_counts(kernel):
     return json.load(open(p)) if os.path.exists(p) else None
 
 
+def launch_report(eng, reps=5):
+    """The engine's launch shapes (the autotuner's table entry for its
+    workload class, or the defaults) and the roofline batch's time with them
+    and with the defaults (ms per evaluation, median of `reps`)."""
+    import ctypes as C
+    from autoscoper_gb300 import _lib as L, tune
+    cls = (C.c_int * 3)()
+    L.call("asc_engine_workload_class", eng.handle, cls)
+    cur = L.LaunchConfig()
+    L.call("asc_engine_get_launch", eng.handle, C.byref(cur), None)
+    mine = (cur.ray_blocks_per_sm, cur.view_blocks_per_sm, cur.ray_shape)
+    rng = np.random.default_rng(3)
+    bones = np.repeat(np.arange(3), 100).astype(np.int32)
+    man = np.concatenate([rng.uniform(-5, 5, (300, 3)), rng.uniform(-5, 5, (300, 3))], 1)
+    t_default = tune.time_config(eng, bones, man, tune.DEFAULT, reps)
+    t_tuned = tune.time_config(eng, bones, man, mine, reps)
+    return {"class": list(cls), "tuned": list(mine), "default": list(tune.DEFAULT),
+            "batch_ms_tuned": t_tuned["total"], "batch_ms_default": t_default["total"],
+            "table": "autoscoper_gb300/tuning.txt" if os.path.exists(L.TUNING) else None}
+
+
 def device_sms():
     import torch
     return torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
@@ -331,6 +352,9 @@ def main():
     L.call("asc_device_sync")
     e2e_s = allmax(pg, (time.perf_counter() - t0) / args.steps)
     e2e = ws * evals_per_step / e2e_s if not args.no_e2e else None
+    # ---- launch shapes: the tuning table's choice for this workload class
+    # against the defaults, on the roofline batch
+    launch = launch_report(eng)
     # ---- roofline of the dominant kernel (ray cast) on one PSO-iteration batch
     L.call("asc_engine_profile", eng.handle, 1)
     rng = np.random.default_rng(3)
@@ -377,6 +401,7 @@ def main():
                 "gpu_launches": args.steps * (1 + 5 * iters),
                 "roofline": rl,
                 "kernel_ms": {"setup": phase[0], "ray": phase[1], "view": phase[2]},
+                "launch": launch,
                 "work": {"samples_per_batch": samples.value, "marched_per_batch": marched,
                          "pixels_per_batch": pixels.value, "batch": nb * npart},
                 "plain": {"value": plain_v, "unit": "pose-evals/s",
@@ -458,8 +483,11 @@ def run_tracking(args):
 
 def run_serving(args):
     """Poisson stream (`--rate` jobs/s, `--jobs` jobs) of mixed registration
-    jobs: continuous batching (4 slots, HBM budget 150 GB, subject volume
-    cache) against the FIFO loop."""
+    jobs, served with continuous batching (up to `--max-jobs` jobs admitted at
+    once, their candidates scored together in every engine launch; HBM
+    budget 150 GB; subject volume cache) and by the FIFO loop (one job at a
+    time) on the same engine.  Latency percentiles over all jobs and over the
+    steady part of the stream (jobs arriving after the first quarter)."""
     from autoscoper_gb300 import _lib as L, api, serve
     L.load()
 
@@ -474,17 +502,27 @@ def run_serving(args):
                                       render_targets=api.render_targets))
         return out
 
+    def steady(js):
+        t_q = sorted(j.arrival for j in js)[len(js) // 4]
+        lat = np.array([j.latency for j in js if j.arrival >= t_q and j.error is None])
+        return {"p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+                "jobs": int(len(lat))}
+
     res = {}
-    for name, slots in (("continuous", 4), ("fifo", 1)):
+    for name, mj in (("continuous", args.max_jobs), ("fifo", 1)):
         js = jobs()
-        summary = serve.Server(hbm_budget=150e9, slots=slots).serve(js, realtime=True)
+        srv = serve.Server(hbm_budget=150e9, max_jobs=mj)
+        summary = srv.serve(js, realtime=True)
+        summary["steady"] = steady(js)
+        summary["jobs_per_s"] = len(js) / summary["wall_s"]
         res[name] = summary
+        del srv
     c, f = res["continuous"], res["fifo"]
     return {"workload": "serving", "metric": "sustained pose evals/s; p50/p99 job latency",
             "value": c["pose_evals_per_s"], "unit": "pose-evals/s", "rate_jobs_per_s": args.rate,
             "continuous": c, "fifo": f, "speedup_vs_fifo": c["pose_evals_per_s"] / max(f["pose_evals_per_s"], 1e-9),
             "data": f"synthetic mixed jobs: volumes 64^3-320^3 u16, viewports 256^2-1024^2, 1-4 bones, 1-3 views, "
-                    f"1-{args.max_frames} frames, PSO 32-128 particles x {args.pso_iters} iterations"}
+                    f"1-{args.max_frames} frames, PSO 32-128 particles x {args.pso_iters} iterations then simplex"}
 
 
 def run_precision(args):
@@ -656,6 +694,7 @@ if __name__ == "__main__":
         ap.add_argument("--oracle-sample", type=int, default=12)
         ap.add_argument("--max-frames", type=int, default=5, help="serving: frames per job drawn from 1..max")
         ap.add_argument("--pso-iters", type=int, default=10, help="serving: PSO iterations per frame")
+        ap.add_argument("--max-jobs", type=int, default=8, help="serving: jobs admitted at once")
         ap.add_argument("--particles", type=int, default=100, help="roofline: candidates per bone")
         ap.add_argument("--reps", type=int, default=3, help="roofline: evaluations")
         ap.add_argument("--storage", default="u16", choices=["u16", "f16", "bf16", "f32"],

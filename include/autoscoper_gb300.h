@@ -241,13 +241,51 @@ typedef struct {
 } asc_bone_desc;
 
 /* cf_model (Tracker::optimize's cf_model, Tracker.cpp:762-770): 0 scores a
- * view by 1 - NCC, 1 by the SAD of gpu::hdist (HDist_kernels.cu:111-203). */
+ * view by 1 - NCC, 1 by the SAD of gpu::hdist (HDist_kernels.cu:111-203).
+ * Up to 16 views and 64 bones; each bone is scored in the first
+ * min(n_views, 4) views (asc_engine_set_bone picks others). */
 int asc_engine_create(int n_views, const asc_view_desc *views, int n_bones, const asc_bone_desc *bones,
                       int render_width, int render_height, int max_items, int coverage, int cf_model,
                       asc_engine *out);
 int asc_engine_destroy(asc_engine e);
 int asc_engine_set_base_pose(asc_engine e, int bone, const double xyzypr[6]);
 int asc_engine_set_radiograph(asc_engine e, int view, asc_image radiograph);
+/* Serving: an engine's views and bones as slots that hold different jobs
+ * over its lifetime (no counterpart in the reference, which holds one trial).
+ * asc_engine_set_view replaces view `view` (camera, radiograph, background,
+ * filter lists) and gives it its own render size (at most the engine's);
+ * asc_engine_set_bone replaces bone `bone` (volume, pivot, base pose) and
+ * scores it in engine views views[0 .. n_views) with desc->step/intensity/
+ * cutoff[j] in views[j] (n_views at most min(the engine's views, 4)).  A
+ * candidate of a bone is then scored in that bone's views only, so one batch
+ * mixes bones of different jobs (cameras, radiographs, filters, render sizes).
+ * Call between evaluations (they copy to the device synchronously); engines
+ * with bones moved to other views serve asc_engine_eval / _eval_host and the
+ * optimizers, and their plain path and image exports return ASC_ERR_STATE.
+ * view_cost outputs hold min(n_views of the engine, 4) entries per candidate,
+ * in the order of the bone's views, 0 past its last. */
+int asc_engine_set_view(asc_engine e, int view, const asc_view_desc *desc, int render_width, int render_height);
+int asc_engine_set_bone(asc_engine e, int bone, const asc_bone_desc *desc, int n_views, const int *views);
+/* Launch shapes of an engine's evaluation (no counterpart in the
+ * reference): blocks per SM of the ray-cast kernel (1..4) and of the
+ * filter/NCC kernel (0: as many as fit), and the ray block each warp of a
+ * 16 x 16 ray tile takes (2: 4 x 8 rays, 3: 8 x 4, 4: 16 x 2).  Results do
+ * not depend on them.  asc_engine_create applies the loaded tuning table's
+ * entry for the engine's workload class (asc_engine_workload_class: ceil
+ * log2 of the render pixels, ceil log2 of the largest volume's voxels, the
+ * views), else the defaults {4, 0, 3}.  asc_tuning_load reads the table the
+ * project's autotuner writes (autoscoper_gb300/tuning.txt: lines of
+ * "rpx vox views ray_blocks view_blocks ray_shape", '#' comments) and
+ * replaces the loaded one; engines created before keep their shapes. */
+typedef struct {
+  int ray_blocks_per_sm;
+  int view_blocks_per_sm;
+  int ray_shape;
+} asc_launch_config;
+int asc_engine_set_launch(asc_engine e, const asc_launch_config *cfg);
+int asc_engine_get_launch(asc_engine e, asc_launch_config *cfg, int *view_blocks_max);
+int asc_engine_workload_class(asc_engine e, int out[3]);
+int asc_tuning_load(const char *path);
 /* RayCaster::setVisible for one bone in every view (the volume visibility
  * of AutoscoperMainWindow::setVolumeVisibility): a hidden bone renders an
  * all-zero DRR, so its views score the empty-mask cost. */

@@ -156,3 +156,18 @@ def test_pose_curve_reads(lib):
     assert c.keys(4) == 15 and c.keys(5) == 0
     c.erase(4, 8)
     assert c.keys(4) == 7 and np.array_equal(c.eval(4)[3:], np.zeros(3))
+
+
+def test_tuning_table_parses(tmp_path):
+    """asc_tuning_load reads the autotuner's table (host only) and rejects a
+    malformed line; the committed table parses."""
+    lib = _lib.load()
+    good = tmp_path / "t.txt"
+    good.write_text("# comment\n20 23 2 4 0 3  # headline\n\n18 21 2 3 2 2\n")
+    assert lib.asc_tuning_load(str(good).encode()) == _lib.ASC_OK
+    bad = tmp_path / "b.txt"
+    bad.write_text("20 23 2 9 0 3\n")  # 9 ray blocks per SM: out of range
+    assert lib.asc_tuning_load(str(bad).encode()) == -1
+    assert lib.asc_tuning_load(str(tmp_path / "missing.txt").encode()) == -1
+    if os.path.exists(_lib.TUNING):
+        assert lib.asc_tuning_load(_lib.TUNING.encode()) == _lib.ASC_OK

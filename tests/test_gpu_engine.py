@@ -213,3 +213,22 @@ def test_hidden_bone_scores_the_empty_mask(scene):
     eng.set_visible(0, True)
     again, _ = eng.eval(bones, man)
     assert np.array_equal(again, before)
+
+
+def test_launch_shapes_change_no_result(scene):
+    """The autotuner's launch shapes (ray-cast blocks per SM, a warp's ray
+    block, filter blocks per SM) change times only: every shape gives the
+    same costs to the bit."""
+    import ctypes as C
+    sc, tr = scene
+    eng = api.Engine(sc, max_items=32)
+    rng = np.random.default_rng(17)
+    bones, man = _cands(rng, 24, len(sc.volumes))
+    want, wantv = eng.eval(bones, man)
+    for cfg in ((4, 0, 2), (3, 1, 4), (2, 2, 3), (1, 1, 2)):
+        c = L.LaunchConfig(*cfg)
+        L.call("asc_engine_set_launch", eng.handle, C.byref(c))
+        got, gotv = eng.eval(bones, man)
+        assert np.array_equal(got, want) and np.array_equal(gotv, wantv), cfg
+    bad = L.LaunchConfig(5, 0, 3)
+    assert L.load().asc_engine_set_launch(eng.handle, C.byref(bad)) == -1

@@ -1,11 +1,14 @@
-"""Serving loop: jobs admitted by an HBM budget, run concurrently on their
-own streams, return exactly the poses they return when run alone."""
+"""Serving loop: jobs admitted by slots and an HBM budget, their candidates
+scored together in shared engine launches, return exactly the poses they
+return when run alone; admission keeps the reserved bytes under the budget."""
 import numpy as np
 import pytest
 
 from autoscoper_gb300 import api, serve
 
 pytestmark = pytest.mark.gpu
+
+RENDER = (192, 192)
 
 
 def _jobs():
@@ -21,24 +24,41 @@ def _jobs():
 
 def test_results_same_alone_and_in_mix():
     alone = _jobs()
+    launches_alone = 0
     for j in alone:
-        serve.Server(hbm_budget=150e9, slots=1).serve([j], realtime=False)
+        srv = serve.Server(hbm_budget=150e9, max_jobs=1, render=RENDER, max_items=512)
+        launches_alone += srv.serve([j], realtime=False)["launches"]
     mixed = _jobs()
-    summary = serve.Server(hbm_budget=150e9, slots=4).serve(mixed, realtime=False)
+    srv = serve.Server(hbm_budget=150e9, max_jobs=4, render=RENDER, max_items=512)
+    summary = srv.serve(mixed, realtime=False)
     assert summary["failed"] == 0, [j.error for j in mixed]
     assert summary["cache_hits"] >= 1  # subject "a" twice
+    # the jobs shared launches: far fewer than the jobs alone needed
+    assert summary["launches"] < 0.6 * launches_alone, (summary["launches"], launches_alone)
     for a, m in zip(alone, mixed):
         assert a.error is None and m.error is None
         assert len(a.poses) == len(m.poses) == a.frames
         for pa, pm in zip(a.poses, m.poses):
             assert np.array_equal(pa, pm)
+        assert a.evals == m.evals
+
+
+def test_registration_moves_towards_truth():
+    job = _jobs()[1]
+    serve.Server(hbm_budget=150e9, max_jobs=1, render=RENDER, max_items=512).serve([job], realtime=False)
+    truth = np.array([np.asarray(t, np.float64) for t in job.scene.truth])
+    start = np.array([np.asarray(p, np.float64) for p in job.scene.poses])
+    final = job.poses[-1]
+    assert np.abs(final[:, :3] - truth[:, :3]).mean() < np.abs(start[:, :3] - truth[:, :3]).mean()
 
 
 def test_admission_respects_budget():
     jobs = _jobs()
-    need = max(serve.engine_bytes(j.scene, len(j.scene.volumes) * j.particles) for j in jobs)
-    budget = 1.5 * need + 2e9  # room for about one job at a time
-    srv = serve.Server(hbm_budget=budget, slots=4)
+    probe = serve.Server(hbm_budget=150e9, max_jobs=4, render=RENDER, max_items=512)
+    need = max(sum(serve.volume_bytes(v) for v in j.scene.volumes) + serve.job_bytes(j) for j in jobs)
+    budget = probe.base_bytes + 1.5 * need  # room for about one job at a time
+    del probe
+    srv = serve.Server(hbm_budget=budget, max_jobs=4, render=RENDER, max_items=512)
     summary = srv.serve(jobs, realtime=False)
     assert summary["failed"] == 0, [j.error for j in jobs]
     assert srv.peak <= budget
