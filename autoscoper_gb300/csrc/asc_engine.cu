@@ -78,7 +78,8 @@ struct BoneDev {
   double pivot[12], pivot_inv[12], base[6];
   // per slot: the bone is scored in views view_of[0 .. n_slots), with that
   // view's RayCaster settings and its empty-cell grid
-  float step[MAX_SLOTS], scale[MAX_SLOTS], cutoff_raw[MAX_SLOTS];
+  float step[MAX_SLOTS], scale[MAX_SLOTS];
+  Cutoff cut[MAX_SLOTS];
   const uint8_t* occ[MAX_SLOTS];
   int view_of[MAX_SLOTS];
   int n_slots;
@@ -320,7 +321,7 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
 // single ray.  A ray with more than NBW segments takes further passes.
 template <int STORE>
 __device__ __forceinline__ void march_segments(const DevVolume& V, const float4 (*rec)[NRAY], const unsigned* ord,
-                                               float* part, int nseg, int* grab, float cut,
+                                               float* part, int nseg, int* grab, const Cutoff& cut,
                                                unsigned long long& marched, unsigned long long& slots)
 {
   const unsigned FULL = 0xffffffffu;
@@ -390,7 +391,7 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
     const bool valid = x < r.w && y < r.h;
     const BoneDev& B = sc->bones[r.bone];
     const int j = r.slot;
-    const float cut = B.cutoff_raw[j];
+    const Cutoff& cut = B.cut[j];
     const uint8_t* occ = skip ? B.occ[j] : nullptr;
     RaySetup rs{};
     const bool hit = valid && ray_setup(r.m, r.vp, x, y, df{r.sx[0], r.sx[1]}, df{r.sy[0], r.sy[1]}, B.step[j],
@@ -1293,6 +1294,26 @@ static void set_base(BoneDev& B, const double* xyzypr) { memcpy(B.base, xyzypr, 
 
 namespace {
 void apply_tuning(asc_engine_s* e);  // the tuning table's launch shapes, below
+
+// k_view's dynamic shared-memory limit is an attribute of the function, one
+// per device for the whole process: it only ever grows here, so an engine
+// with a narrower filter chain never lowers it below what an earlier engine
+// launches with.
+std::mutex g_view_smem_mu;
+size_t g_view_smem[64] = {};
+
+cudaError_t ensure_view_smem(size_t bytes)
+{
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err) return err;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> l(g_view_smem_mu);
+  if (bytes <= g_view_smem[dev]) return cudaSuccess;
+  err = cudaFuncSetAttribute(k_view, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (!err) g_view_smem[dev] = bytes;
+  return err;
+}
 }
 
 ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bones, const asc_bone_desc* bones,
@@ -1351,13 +1372,13 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
       B.view_of[j] = j;
       B.step[j] = bones[i].step[j];
       B.scale[j] = bones[i].step[j] * vh->dev.norm / bones[i].intensity[j];
-      B.cutoff_raw[j] = bones[i].cutoff[j] / vh->dev.norm;
+      B.cut[j] = make_cutoff(bones[i].cutoff[j], vh->dev.norm);
       uint8_t* occ = nullptr;
       if (e->alloc(occ, occ_grid_bytes(occupancy_cells(vh->dev)))) {
         delete e;
         return ASC_ERR_NOMEM;
       }
-      build_occupancy(vh->dev, B.cutoff_raw[j], occ, cs);
+      build_occupancy(vh->dev, B.cut[j].lo, occ, cs);
       B.occ[j] = occ;
     }
   }
@@ -1410,7 +1431,7 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, dev);
-  err = cudaFuncSetAttribute(k_view, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem);
+  err = ensure_view_smem(e->smem);
   if (!err) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e->view_blocks, k_view, VNT, e->smem);
   if (err) {
     delete e;
@@ -1479,7 +1500,7 @@ ASC_API int asc_engine_set_view(asc_engine e, int view, const asc_view_desc* des
   const size_t need = view_smem_floats(d.E) * sizeof(float);
   if (need > e->smem) {  // a wider filter chain than the engine's views had so far
     int blocks = 0;
-    ASC_CUDA(cudaFuncSetAttribute(k_view, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+    ASC_CUDA(ensure_view_smem(need));
     ASC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_view, VNT, need));
     e->smem = need;
     e->view_blocks = std::max(blocks, 1);
@@ -1518,7 +1539,7 @@ ASC_API int asc_engine_set_bone(asc_engine e, int bone, const asc_bone_desc* des
     B.view_of[j] = views[j];
     B.step[j] = desc->step[j];
     B.scale[j] = desc->step[j] * vh->dev.norm / desc->intensity[j];
-    B.cutoff_raw[j] = desc->cutoff[j] / vh->dev.norm;
+    B.cut[j] = make_cutoff(desc->cutoff[j], vh->dev.norm);
     uint8_t*& occ = e->occ_own[bone][j];
     if (e->occ_cap[bone][j] < grid) {
       if (occ) cudaFree(occ);
@@ -1527,7 +1548,7 @@ ASC_API int asc_engine_set_bone(asc_engine e, int bone, const asc_bone_desc* des
       ASC_CUDA(cudaMalloc(&occ, grid));
       e->occ_cap[bone][j] = grid;
     }
-    build_occupancy(vh->dev, B.cutoff_raw[j], occ, nullptr);
+    build_occupancy(vh->dev, B.cut[j].lo, occ, nullptr);
     B.occ[j] = occ;
   }
   ASC_CUDA(cudaStreamSynchronize(nullptr));

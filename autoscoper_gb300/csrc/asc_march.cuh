@@ -379,6 +379,36 @@ __device__ __host__ __forceinline__ void df_split(double d, float& h, float& l)
   l = (float)(d - (double)h);
 }
 
+// The cutoff test of the march (RayCaster_kernels.cu:189: density += s >
+// cutoff ? step * s : 0), on raw voxel values.  An FP32 sample can differ
+// from the exact trilinear value of its exact position by up to ~1 raw unit
+// (sample positions carry ~5e-6 voxel of rounding; a step of 65535 between
+// neighbouring voxels turns that into 0.33 per axis), so a sample within
+// that much of the cutoff could fall on the other side of it than the exact
+// computation.  Samples in (lo, hi) are therefore decided again from their
+// double-float position and a double-float trilinear value against the
+// exact threshold c x vmax (c the normalized cutoff, vmax 65535 or 255: the
+// reference compares raw / vmax with c); all others are decided in FP32.
+// `raw` (c / norm) is the FP32 threshold of the occupancy grids, which are
+// built at `lo` so that every cell holding a voxel that a sample decided
+// exactly could count stays marched.
+struct Cutoff {
+  float raw, lo, hi;
+  float th, tl;  // c x vmax as a double-float
+};
+
+__host__ __device__ inline Cutoff make_cutoff(float c, float norm)
+{
+  Cutoff k;
+  k.raw = c / norm;
+  const float tol = 1.0f + 1e-5f * fabsf(k.raw);
+  k.lo = k.raw - tol;
+  k.hi = k.raw + tol;
+  const double vmax = (double)(int)(1.0f / norm + 0.5f);
+  df_split((double)c * vmax, k.th, k.tl);
+  return k;
+}
+
 // Per-ray set-up of cuda_volume_render_kernel (RayCaster_kernels.cu:144-186)
 // for pixel (x, y) of an image over viewport `vp`, with camera->volume matrix
 // m (3x4 row-major, normalisation folded), in double-float: the reference's
@@ -632,16 +662,61 @@ __device__ __forceinline__ void coord_base(df C, df dC, float k, int& base_i, fl
   frac = __fadd_rn(__fadd_rn(c.h, -fl), c.l);
 }
 
+// Whether sample k of a ray (texel coordinates X - k dX etc. as double-floats)
+// lies above the cutoff, computed exactly enough to agree with FP64: the
+// position and the trilinear value in double-float, against the threshold
+// (th, tl).  The rare slow path of the cutoff test (Cutoff); kept out of line
+// so that the march's registers do not pay for it.
+template <int STORE>
+__device__ __noinline__ bool sample_above(const DevVolume& V, float Xh, float Xl, float Yh, float Yl, float Zh,
+                                          float Zl, float dXh, float dXl, float dYh, float dYl, float dZh, float dZl,
+                                          int k, float th, float tl)
+{
+  const float kf = (float)k;
+  const df C[3] = {df_add(df{Xh, Xl}, df_neg(df_mulf(df{dXh, dXl}, kf))),
+                   df_add(df{Yh, Yl}, df_neg(df_mulf(df{dYh, dYl}, kf))),
+                   df_add(df{Zh, Zl}, df_neg(df_mulf(df{dZh, dZl}, kf)))};
+  int b[3];
+  df f[3];
+  for (int i = 0; i < 3; ++i) {
+    float fl = floorf(C[i].h);
+    if (fl == C[i].h && C[i].l < 0.f) fl -= 1.0f;  // h + l lies just below the integer h
+    fl = fminf(fmaxf(fl, -1.0f), 1.0e6f);
+    b[i] = (int)fl;
+    f[i] = df_two_sum(__fadd_rn(C[i].h, -fl), C[i].l);  // C - floor(C): h - floor(h) is exact
+  }
+  const unsigned px = (unsigned)V.px, pxy = (unsigned)V.pxy;
+  const unsigned imax = ASC_QUADS ? (unsigned)(V.nz + 2 * PAD - 1) * pxy - 1u
+                                  : (unsigned)(V.nz + 2 * PAD - 1) * pxy - px - 1u;
+  const unsigned i = min((unsigned)(b[2] + PAD) * pxy + (unsigned)(b[1] + PAD) * px + (unsigned)(b[0] + PAD), imax);
+  const Taps<STORE> t = fetch_taps<STORE>(V.pairs, i, px, pxy);
+  df e[4];
+  for (int q = 0; q < 4; ++q) {
+    float lo, hi;
+    if constexpr (STORE == ASC_STORE_F32) {
+      lo = t.p[q].x;
+      hi = t.p[q].y;
+    } else {
+      unpack<STORE>(t.w[q], lo, hi);
+    }
+    e[q] = df_add(df{lo, 0.f}, df_mulf(f[0], __fadd_rn(hi, -lo)));  // raw values: hi - lo is exact
+  }
+  const df f0 = df_add(e[0], df_mul(f[1], df_add(e[1], df_neg(e[0]))));
+  const df f1 = df_add(e[2], df_mul(f[1], df_add(e[3], df_neg(e[2]))));
+  const df v = df_add(f0, df_mul(f[2], df_add(f1, df_neg(f0))));
+  return df_lt(df{th, tl}, v);
+}
+
 // Samples kb + js .. kb + je of one march block (kb a multiple of REBASE) of
 // cuda_volume_render_kernel's loop (RayCaster_kernels.cu:187-195; t = far -
-// k).  Returns the block's FP32 sum of raw samples above cutoff_raw (at most
+// k).  Returns the block's FP32 sum of raw samples above the cutoff (at most
 // REBASE of them, so its relative error stays below ~4e-6 and typically near
 // 1e-7; the blocks are combined in double-float); a sample at or below the
 // cutoff leaves it untouched, so trimming samples that add nothing changes no
 // bit.
 template <int STORE>
 __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup& r, int kb, int js, int je,
-                                              float cutoff_raw)
+                                              const Cutoff& cut)
 {
   const uint32_t* __restrict__ P = V.pairs;
   const unsigned px = (unsigned)V.px, pxy = (unsigned)V.pxy;
@@ -677,8 +752,13 @@ __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup&
     az = __fadd_rn(Z, -__fadd_rn(tz, -M));
     return min(__float_as_uint(tz) * pxy + __float_as_uint(ty) * px + __float_as_uint(tx) + i_base, imax);
   };
+  // the exact cutoff test of sample ks (Cutoff), for values near the cutoff
+  auto exact = [&](int ks) {
+    return sample_above<STORE>(V, r.X.h, r.X.l, r.Y.h, r.Y.l, r.Z.h, r.Z.l, r.dX.h, r.dX.l, r.dY.h, r.dY.l, r.dZ.h,
+                               r.dZ.l, ks, cut.th, cut.tl);
+  };
   // one sample's trilinear value from its taps, added when above the cutoff
-  auto accumulate = [&](const Taps<STORE>& t, float wx, float wy, float wz) {
+  auto accumulate = [&](const Taps<STORE>& t, float wx, float wy, float wz, int ks) {
     const float e00 = lerp_tap<STORE>(t, 0, wx);
     const float e10 = lerp_tap<STORE>(t, 1, wx);
     const float e01 = lerp_tap<STORE>(t, 2, wx);
@@ -686,7 +766,7 @@ __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup&
     const float f0 = fmaf(wy, e10 - e00, e00);
     const float f1 = fmaf(wy, e11 - e01, e01);
     const float v = fmaf(wz, f1 - f0, f0);
-    if (v > cutoff_raw) acc += v;
+    if (v > cut.lo && (v >= cut.hi || exact(ks))) acc += v;
   };
   // Samples two at a time (jj and jj + 1) in packed pairs, both samples'
   // loads issued together; the samples add in order.
@@ -709,14 +789,14 @@ __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup&
     locate2(j, wx, wy, wz, ia, ib);
     const Taps<STORE> A = fetch_taps<STORE>(P, ia, px, pxy), B = fetch_taps<STORE>(P, ib, px, pxy);
     const float2 v = trilinear2<STORE>(A, B, wx, wy, wz);
-    if (v.x > cutoff_raw) acc += v.x;
-    if (v.y > cutoff_raw) acc += v.y;
+    if (v.x > cut.lo && (v.x >= cut.hi || exact(kb + k))) acc += v.x;
+    if (v.y > cut.lo && (v.y >= cut.hi || exact(kb + k + 1))) acc += v.y;
     j += 2.0f;
   }
   if (k == je) {
     float ax, ay, az;
     const Taps<STORE> A = fetch_taps<STORE>(P, locate(j, ax, ay, az), px, pxy);
-    accumulate(A, ax, ay, az);
+    accumulate(A, ax, ay, az, kb + k);
   }
   return acc;
 }
@@ -734,7 +814,7 @@ __device__ __forceinline__ void add_block(df& total, float p)
 // with and without `occ`, and the same as the batched engine's.
 template <int STORE>
 __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __restrict__ occ, const RaySetup& r,
-                                       float cutoff_raw)
+                                       const Cutoff& cut)
 {
   if (r.K <= 0) return 0.f;
   CellWalk w = cell_walk(V, r, 0);
@@ -745,7 +825,7 @@ __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __rest
     ia = t.ia[i];
     c = t.c[i];
   }, s, [&](int kb, int js, int je) {
-    add_block(total, march_block<STORE>(V, r, kb, js, je, cutoff_raw));
+    add_block(total, march_block<STORE>(V, r, kb, js, je, cut));
     return true;
   });
   return total.h + total.l;

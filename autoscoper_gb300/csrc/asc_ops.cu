@@ -53,7 +53,8 @@ int gauss_1d(float radius, float* g, int cap)
 struct RayArgs {
   float m[12];
   float vp[4];
-  float step, scale, cutoff_raw;
+  float step, scale;
+  Cutoff cut;
   float sx[2], sy[2];  // vp[2] / w and vp[3] / h as double-floats
 };
 
@@ -68,7 +69,7 @@ __global__ void __launch_bounds__(256) k_raycast(DevVolume V, const uint8_t* __r
   RaySetup r;
   float d = 0.f;
   if (ray_setup(a.m, a.vp, x, y, df{a.sx[0], a.sx[1]}, df{a.sy[0], a.sy[1]}, a.step, V.nx, V.ny, V.nz, r))
-    d = march<STORE>(V, occ, r, a.cutoff_raw) * a.scale;
+    d = march<STORE>(V, occ, r, a.cut) * a.scale;
   out[(size_t)y * w + x] = fminf(fmaxf(d, 0.f), 1.f);
 }
 
@@ -834,7 +835,7 @@ int raycast_launch(const DevVolume& V, const uint8_t* occ, const float* m12, con
   a.step = step;
   // density = step * sum(norm * raw) / intensity; cutoff compares normalized samples
   a.scale = step * V.norm / intensity;
-  a.cutoff_raw = cutoff / V.norm;
+  a.cut = make_cutoff(cutoff, V.norm);
   df_split((double)vp[2] / (double)w, a.sx[0], a.sx[1]);
   df_split((double)vp[3] / (double)h, a.sy[0], a.sy[1]);
   dim3 grid((w + 15) / 16, (h + 15) / 16);
@@ -866,7 +867,7 @@ ASC_API int asc_raycast(asc_volume vol, const double imv[16], const float vp[4],
   fold_matrix(imv, v->inv_scale, v->inv_trans, m);
   const uint8_t* occ = nullptr;
   if (g_empty_skip) {
-    const float cut = cutoff / v->dev.norm;
+    const float cut = make_cutoff(cutoff, v->dev.norm).lo;  // the occupancy grid's threshold
     if (!v->occ) {
       Gate g(device_gate());
       ASC_CUDA(cudaMalloc(&v->occ, occ_grid_bytes(occupancy_cells(v->dev))));

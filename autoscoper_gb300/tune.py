@@ -152,7 +152,11 @@ def main(argv=None):
 
     results["serving: 6 mixed jobs on a 16-view slot engine, one PSO iteration each"] = tune(_E, b, m, a.reps)
     write_table(a.out, results)
-    print(json.dumps({k: {kk: v for kk, v in r.items() if kk != "runs"} for k, r in results.items()}))
+    out = {}
+    for k, r in results.items():
+        out[k] = {kk: v for kk, v in r.items() if kk != "runs"}
+        out[k]["runs"] = sorted([[*x["cfg"], round(x["total"], 3)] for x in r["runs"]], key=lambda x: x[-1])
+    print(json.dumps(out))
 
 
 if __name__ == "__main__":

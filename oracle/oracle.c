@@ -574,6 +574,7 @@ ORC_EXPORT void orc_raycast(const void *vol, int vtype, int nx, int ny, int nz, 
 ORC_EXPORT void orc_image_render(const void *img, int vtype, int W, int H, const double ip[4], const double vp[4],
                                  int mode, double threshold, double *out, int w, int h)
 {
+#pragma omp parallel for schedule(static)
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       double u = vp[0] + vp[2] * (x / (double)w);
@@ -627,6 +628,7 @@ ORC_EXPORT void orc_composite(const double *s1, const double *s2, const double *
 /* sobel_filter_kernel, SobelFilter_kernels.cu:63-113. */
 ORC_EXPORT void orc_sobel(const double *in, double *out, int w, int h, double scale, double blend)
 {
+#pragma omp parallel for schedule(static)
   for (int y1 = 0; y1 < h; ++y1)
     for (int x1 = 0; x1 < w; ++x1) {
       int x0 = x1 > 0 ? x1 - 1 : 0, y0 = y1 > 0 ? y1 - 1 : 0;
@@ -647,6 +649,7 @@ ORC_EXPORT void orc_sobel(const double *in, double *out, int w, int h, double sc
 /* contrast_filter_kernel + average, ContrastFilter_kernels.cu:62-96. */
 ORC_EXPORT void orc_contrast(const double *in, double *out, int w, int h, double alpha, double beta, int size)
 {
+#pragma omp parallel for schedule(static)
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       int i0 = y - size / 2 > 0 ? y - size / 2 : 0, i1 = y + (size + 1) / 2 < h ? y + (size + 1) / 2 : h;
@@ -702,6 +705,7 @@ static double convolve(const double *in, int w, int h, int x, int y, const doubl
  * GaussianFilter.cpp:130-131 copies a single float). */
 ORC_EXPORT void orc_gaussian(const double *in, double *out, int w, int h, const double *wts, int K)
 {
+#pragma omp parallel for schedule(static)
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       size_t p = (size_t)y * w + x;
@@ -718,6 +722,7 @@ ORC_EXPORT void orc_gaussian(const double *in, double *out, int w, int h, const 
 ORC_EXPORT void orc_sharpen(const double *in, double *out, int w, int h, const double *wts, int K, double contrast,
                             double threshold)
 {
+#pragma omp parallel for schedule(static)
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       size_t p = (size_t)y * w + x;

@@ -9,6 +9,7 @@
 #define __device__
 #define __host__
 #define __forceinline__ inline
+#define __noinline__
 using std::max;
 using std::min;
 inline float __fadd_rn(float a, float b) { volatile float r = a + b; return r; }

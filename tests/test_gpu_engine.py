@@ -232,3 +232,59 @@ def test_launch_shapes_change_no_result(scene):
         assert np.array_equal(got, want) and np.array_equal(gotv, wantv), cfg
     bad = L.LaunchConfig(5, 0, 3)
     assert L.load().asc_engine_set_launch(eng.handle, C.byref(bad)) == -1
+
+
+def test_engines_with_different_chains_coexist():
+    """k_view's shared-memory limit belongs to the function, not the engine:
+    an engine created after one with a wider filter chain must not lower it
+    below what the first launches with."""
+    wide = S.make_scene([(40, 48, 56)], 1.0, (112, 112), 0.9, filters="chain", seed=3)
+    narrow = S.make_scene([(40, 48, 56)], 1.0, (112, 112), 0.9, filters="sobel", seed=3)
+    for sc in (wide, narrow):
+        make_targets(sc, O.Tracker(sc))
+    e_wide = api.Engine(wide, max_items=8)
+    man = np.zeros((2, 6))
+    man[1] = [0.3, -0.2, 0.1, 0.5, 0.2, -0.4]
+    want, _ = e_wide.eval(np.zeros(2, np.int32), man)
+    e_narrow = api.Engine(narrow, max_items=8)
+    e_narrow.eval(np.zeros(2, np.int32), man)
+    got, _ = e_wide.eval(np.zeros(2, np.int32), man)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("coverage", [L.ASC_SUM_TREE, L.ASC_SUM_FULL])
+def test_engine_background_threshold_matches_oracle(coverage):
+    """View::renderBackground with a threshold >= 0 (View.cpp:171-194,
+    BackgroundRenderer_kernels.cu:88-120): the background mask multiplies the
+    DRR mask (Tracker.cpp:744-752).  The fused k_view branch and the plain
+    path against the oracle, per view within the NCC bar; the mask must cut
+    pixels the DRR mask keeps."""
+    sc = S.make_scene([(40, 48, 56), (36, 30, 44)], 1.0, (112, 112), 0.9, filters="chain", seed=19,
+                      bone_offsets=[(0, 0, -12), (4, -3, 14)])
+    tr = O.Tracker(sc)
+    make_targets(sc, tr)
+    yy, xx = np.mgrid[0:112, 0:112]
+    for i, v in enumerate(sc.views):
+        v.background = (0.5 + 0.5 * np.sin(xx / (7.0 + i)) * np.cos(yy / 11.0)).astype(np.float32)
+        v.bg_threshold = 0.35
+    tr = O.Tracker(sc, tree=coverage == L.ASC_SUM_TREE)
+    eng = api.Engine(sc, max_items=32, coverage=coverage)
+    rng = np.random.default_rng(23)
+    bones, man = _cands(rng, 10, len(sc.volumes))
+    cost, vcost = eng.eval(bones, man)
+    pcost, pvcost = eng.eval(bones, man, plain=True)
+    refs = []
+    for k in range(len(bones)):
+        pose = tr.compose(int(bones[k]), man[k])
+        refv = tr.track_frame(int(bones[k]), pose)
+        refs.append(refv)
+        _check(cost[k], tr.minimization_func(int(bones[k]), man[k]), refv)
+        _check(pcost[k], tr.minimization_func(int(bones[k]), man[k]), refv)
+        for v in range(2):
+            for got in (vcost[k, v], pvcost[k, v]):
+                assert abs((1.0 - got) - (1.0 - refv[v])) <= ncc_bar(1.0 - refv[v]), (k, v, got, refv[v])
+    # the threshold matters: without it the oracle scores differently
+    for v in sc.views:
+        v.bg_threshold = -1.0
+    plain = [tr.track_frame(int(bones[k]), tr.compose(int(bones[k]), man[k])) for k in range(len(bones))]
+    assert not np.allclose(np.array(plain), np.array(refs), rtol=1e-3, atol=0)

@@ -191,3 +191,39 @@ def test_ncc_degenerate():
     z = api.DeviceArray.from_host(np.zeros(64, np.float32))
     one = api.DeviceArray.from_host(np.ones(64, np.float32))
     assert api.ncc(z, z, one) == 1e5
+
+
+def test_cutoff_at_a_voxel_level_decides_as_fp64():
+    """A cutoff exactly at a tissue level (c = float32(200 / 65535), which FP32
+    alone would round to the level itself): the plain ray caster and the
+    batched engine count every sample of the uniform 200 soft tissue, as the
+    FP64 oracle does (RayCaster_kernels.cu:189), and the engine's costs stay
+    within the NCC bar."""
+    sc = S.make_scene([(40, 36, 44)], 1.0, (96, 96), 1.0, filters="sobel", seed=4)
+    sc.volumes[0].data = S.phantom((40, 36, 44), seed=4, noise=0.0)
+    cut = float(np.float32(200.0 / 65535.0))
+    for row in sc.ray:
+        row[0].cutoff = cut
+    tr = O.Tracker(sc)
+    for vi, v in enumerate(sc.views):
+        ok, m, _, _, _ = tr.view_setup(0, vi, sc.truth[0])
+        drr = O.raycast(tr.vd[0], m, S.target_viewport(v.camera), sc.ray[vi][0].step, sc.ray[vi][0].intensity, cut,
+                        96, 96)
+        v.radiograph = S.radiograph_from_drr(drr, seed=vi)
+    dv = api.DeviceVolume(sc.volumes[0])
+    rng = np.random.default_rng(6)
+    pose = S.perturb(sc.truth[0], rng, 2.0, 10.0).astype(np.float64)
+    for vi in range(2):
+        ok, m, vp, w, h = tr.view_setup(0, vi, pose)
+        rp = sc.ray[vi][0]
+        got = api.raycast(dv, _imv(sc, vi, pose), vp, rp.step, rp.intensity, cut, w, h).to_host()
+        ref = O.raycast(tr.vd[0], m, np.float32(vp).astype(np.float64), float(np.float32(rp.step)),
+                        float(np.float32(rp.intensity)), cut, w, h)
+        assert ref.max() > 0.1 and np.abs(got - ref).max() < 1e-6
+    eng = api.Engine(sc, max_items=8, volumes=[dv])
+    man = np.array([[0, 0, 0, 0, 0, 0], [0.4, -0.3, 0.2, 1.0, -0.5, 0.6]], np.float64)
+    _, vcost = eng.eval(np.zeros(2, np.int32), man)
+    for k in range(2):
+        refv = tr.track_frame(0, tr.compose(0, man[k]))
+        for v in range(2):
+            assert abs(vcost[k, v] - refv[v]) <= 1e-5 * max(abs(1.0 - refv[v]), 1e-2), (k, v, vcost[k, v], refv[v])

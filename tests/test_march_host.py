@@ -133,3 +133,27 @@ def test_host_march_f32_storage_equals_u16(hm, small):
     b, nb = run(hm, tr.vd[0], m, vp, rp, w, h, storage=3)
     assert np.array_equal(na, nb)
     assert np.array_equal(a, b)
+
+
+def test_cutoff_at_a_voxel_level_decides_as_fp64(hm):
+    """A cutoff at a tissue level exactly (c = float32(200 / 65535)): a sample
+    of a uniform 200 region is 200 raw in FP32, while c / norm rounds to
+    200.0 but c x 65535 is 199.99999995.  The march decides such samples
+    exactly (RayCaster_kernels.cu:189: s > cutoff), as the FP64 oracle does,
+    so every sample of the soft tissue counts and the DRRs agree."""
+    sc = S.make_scene([(40, 36, 44)], 1.0, (96, 96), 1.0, filters="sobel", seed=4)
+    sc.volumes[0].data = S.phantom((40, 36, 44), seed=4, noise=0.0)  # levels exactly 200, 900, 1800
+    tr = O.Tracker(sc)
+    cut = float(np.float32(200.0 / 65535.0))
+    assert np.float32(cut) / (np.float32(1) / np.float32(65535)) == np.float32(200.0)  # FP32 alone would exclude 200
+    rng = np.random.default_rng(6)
+    for _ in range(2):
+        pose = S.perturb(sc.truth[0], rng, 2.0, 10.0).astype(np.float64)
+        for vi in range(2):
+            ok, m, vp, w, h = tr.view_setup(0, vi, pose)
+            rp = sc.ray[vi][0]
+            got, _ = run(hm, tr.vd[0], m, vp, rp, w, h, cutoff=cut)
+            ref = O.raycast(tr.vd[0], m, np.float32(vp).astype(np.float64), float(np.float32(rp.step)),
+                            float(np.float32(rp.intensity)), cut, w, h)
+            assert ref.max() > 0.1
+            assert np.abs(got - ref).max() < 1e-6
