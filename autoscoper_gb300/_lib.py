@@ -121,6 +121,7 @@ SIGNATURES = {
     "asc_engine_profile": (i32, [vp, i32]),
     "asc_engine_stats": (i32, [vp, P(f32), P(C.c_ulonglong), P(C.c_ulonglong)]),
     "asc_engine_counters": (i32, [vp, P(C.c_ulonglong)]),
+    "asc_engine_exact_rays": (i32, [vp, P(i32)]),
     "asc_engine_pso": (i32, [vp, i32, i32, f64, f64, f64, f64, f64, C.c_uint64, P(f64), P(f64),
                              P(C.c_longlong), vp]),
     "asc_engine_pso_stall": (i32, [vp, i32, i32, i32, f64, f64, f64, f64, f64, C.c_uint64, P(f64), P(f64),

@@ -2,12 +2,15 @@
 // for many (bone, manipulator) candidates per pass, with the scene resident
 // on the device.
 //
-// One evaluation is four launches on one stream (five with cf_model 1):
+// One evaluation is five launches on one stream (six with cf_model 1):
 //   k_setup_iv    a thread per (item, view): FP64 pose composition, view
 //                            matrix, viewport (Tracker.cpp:603-634) and crop;
 //   k_setup       1 block:  the tile layout of every crop, with prefix sums;
 //   k_ray         persistent: 16x16-ray tiles pulled from an atomic queue,
-//                            DRRs written to a packed buffer;
+//                            DRRs written to a packed buffer; rays with a
+//                            sample within rounding of the cutoff are listed;
+//   k_ray_fix     grid-stride: the listed rays marched again with exact
+//                            cutoff decisions;
 //   k_view        persistent: 48x48 output tiles pulled from a queue; each
 //                            stages DRR and radiograph regions with the chain's
 //                            halo in shared memory, runs both filter chains,
@@ -110,6 +113,8 @@ struct Counters {
   int rtiles, ftiles;
   int rnext, fnext;
   int error;
+  int nfix;   // rays whose march met the cutoff's band (k_ray_fix marches them again)
+  int nfixt;  // ray tiles holding such rays
   int pad;
   unsigned long long samples, pixels;
   unsigned long long marched, slots;  // marched samples, 32 x warp-max span
@@ -127,6 +132,7 @@ struct Bufs {
   double* vcost;   // per iv
   unsigned* ivt;   // per-iv tile tickets
   unsigned* itt;   // per-item view tickets
+  int* fixt;       // ray tiles holding rays to march again exactly (k_ray_fix)
   Counters* C;
 };
 
@@ -291,6 +297,8 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
     b.C->rnext = 0;
     b.C->fnext = 0;
     b.C->error = s_err;
+    b.C->nfix = 0;
+    b.C->nfixt = 0;
     b.C->samples = 0;
     b.C->marched = 0;
     b.C->slots = 0;
@@ -345,7 +353,7 @@ __device__ __forceinline__ void march_segments(const DevVolume& V, const float4 
       r.dY = df{q2.x, q2.y};
       r.dZ = df{q2.z, q2.w};
       const int kb = __float_as_int(part[slot]);  // the block start, until the sum replaces it
-      part[slot] = march_block<STORE>(V, r, kb, js, je, cut);
+      part[slot] = march_block<STORE, false>(V, r, kb, js, je, cut);
       len = je - js + 1;
     }
     const unsigned tot = __reduce_add_sync(FULL, (unsigned)len), mx = __reduce_max_sync(FULL, (unsigned)len);
@@ -355,7 +363,9 @@ __device__ __forceinline__ void march_segments(const DevVolume& V, const float4 
 }
 
 // shape: log2 of the width of the ray block each warp takes in a 16 x 16
-// tile (2: 4 x 8, 3: 8 x 4, 4: 16 x 2), the autotuner's choice.
+// tile (2: 4 x 8, 3: 8 x 4, 4: 16 x 2), the autotuner's choice.  A ray any
+// of whose samples fell in the cutoff's band (march_block) leaves the mark
+// -1 in its DRR pixel, and its tile goes on the fix list for k_ray_fix.
 __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev* __restrict__ sc, Bufs b, int skip,
                                                                  int shape)
 {
@@ -415,6 +425,7 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
     }
     WalkState ws{0, rs.K - 1, 0, -1, 0};
     df total{0.f, 0.f};
+    bool flagged = false;
     for (;;) {
       if (tid < REBASE) s_cnt[tid] = 0;
       if (tid == 0) s_grab = 0;
@@ -467,15 +478,63 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
         march_segments<ASC_STORE_U16>(B.vol, s_rec, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
       __syncthreads();
       // ---- this ray's segments, in order
-      for (int i = 0; i < n; ++i) add_block(total, s_part[tid * NBW + i]);
+      for (int i = 0; i < n; ++i) {
+        const float p = s_part[tid * NBW + i];
+        if (block_flagged(p))
+          flagged = true;
+        else
+          add_block(total, p);
+      }
       if (!__syncthreads_or(!done)) break;
     }
-    if (valid) b.drr[r.pix + (long long)y * r.w + x] = fminf(fmaxf((total.h + total.l) * B.scale[j], 0.f), 1.f);
+    const bool fix = valid && flagged;
+    if (valid)
+      b.drr[r.pix + (long long)y * r.w + x] = fix ? -1.0f : fminf(fmaxf((total.h + total.l) * B.scale[j], 0.f), 1.f);
+    const unsigned fm = __ballot_sync(FULL, fix);
+    if (lane == 0 && fm) atomicAdd(&b.C->nfix, __popc(fm));
+    if (__syncthreads_or(fix) && tid == 0) b.fixt[atomicAdd(&b.C->nfixt, 1)] = tile;
   }
   if (lane == 0 && sampled) atomicAdd(&b.C->samples, sampled);
   if (lane == 0 && slots) {
     atomicAdd(&b.C->marched, marched);
     atomicAdd(&b.C->slots, slots);
+  }
+}
+
+// The marked rays of the tiles on the fix list, marched again with every
+// cutoff decision the exact one (march_pass with EXACT); each overwrites its
+// mark.  A thread per (listed tile, ray); the ray set-up is k_ray's, so the
+// samples are the same.
+__global__ void __launch_bounds__(128) k_ray_fix(const SceneDev* __restrict__ sc, Bufs b, int skip)
+{
+  const long long n = (long long)b.C->nfixt * NRAY;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    const int tile = b.fixt[q / NRAY], p = (int)(q % NRAY);
+    const int k = find_iv(b.roff, b.C->n_iv, tile);
+    const IV& r = b.iv[k];
+    const int t = tile - b.roff[k];
+    const int x = (t % r.rtx) * RTX + (p % RTX), y = (t / r.rtx) * RTY + p / RTX;
+    if (x >= r.w || y >= r.h) continue;
+    float* px = b.drr + r.pix + (long long)y * r.w + x;
+    if (!(*px < 0.f)) continue;
+    const BoneDev& B = sc->bones[r.bone];
+    const int j = r.slot;
+    RaySetup rs;
+    float d = 0.f;
+    if (ray_setup(r.m, r.vp, x, y, df{r.sx[0], r.sx[1]}, df{r.sy[0], r.sy[1]}, B.step[j], B.vol.nx, B.vol.ny,
+                  B.vol.nz, rs) &&
+        rs.K > 0) {
+      const uint8_t* occ = skip ? B.occ[j] : nullptr;
+      if (B.vol.storage == ASC_STORE_F32)
+        d = march_pass<ASC_STORE_F32, true>(B.vol, occ, rs, B.cut[j], nullptr);
+      else if (B.vol.storage == ASC_STORE_BF16)
+        d = march_pass<ASC_STORE_BF16, true>(B.vol, occ, rs, B.cut[j], nullptr);
+      else if (B.vol.storage == ASC_STORE_F16)
+        d = march_pass<ASC_STORE_F16, true>(B.vol, occ, rs, B.cut[j], nullptr);
+      else
+        d = march_pass<ASC_STORE_U16, true>(B.vol, occ, rs, B.cut[j], nullptr);
+    }
+    *px = fminf(fmaxf(d * B.scale[j], 0.f), 1.f);
   }
 }
 
@@ -1372,13 +1431,13 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
       B.view_of[j] = j;
       B.step[j] = bones[i].step[j];
       B.scale[j] = bones[i].step[j] * vh->dev.norm / bones[i].intensity[j];
-      B.cut[j] = make_cutoff(bones[i].cutoff[j], vh->dev.norm);
+      B.cut[j] = make_cutoff(bones[i].cutoff[j], vh->dev.norm, vh->dev.gmax);
       uint8_t* occ = nullptr;
       if (e->alloc(occ, occ_grid_bytes(occupancy_cells(vh->dev)))) {
         delete e;
         return ASC_ERR_NOMEM;
       }
-      build_occupancy(vh->dev, B.cut[j].lo, occ, cs);
+      build_occupancy(vh->dev, occupancy_threshold(B.cut[j]), occ, cs);
       B.occ[j] = occ;
     }
   }
@@ -1399,6 +1458,8 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
   if (!err) err = e->alloc(e->b.vcost, n_iv);
   if (!err) err = e->alloc(e->b.ivt, n_iv);
   if (!err) err = e->alloc(e->b.itt, (size_t)max_items);
+  // at most every ray tile of a full batch
+  if (!err) err = e->alloc(e->b.fixt, n_iv * (size_t)((rw + RTX - 1) / RTX) * ((rh + RTY - 1) / RTY));
   if (!err) err = e->alloc(e->b.C, 1);
   if (!err) err = e->alloc(e->d_bone, (size_t)max_items);
   if (!err) err = e->alloc(e->d_manip, (size_t)max_items * 6);
@@ -1539,7 +1600,7 @@ ASC_API int asc_engine_set_bone(asc_engine e, int bone, const asc_bone_desc* des
     B.view_of[j] = views[j];
     B.step[j] = desc->step[j];
     B.scale[j] = desc->step[j] * vh->dev.norm / desc->intensity[j];
-    B.cut[j] = make_cutoff(desc->cutoff[j], vh->dev.norm);
+    B.cut[j] = make_cutoff(desc->cutoff[j], vh->dev.norm, vh->dev.gmax);
     uint8_t*& occ = e->occ_own[bone][j];
     if (e->occ_cap[bone][j] < grid) {
       if (occ) cudaFree(occ);
@@ -1548,7 +1609,7 @@ ASC_API int asc_engine_set_bone(asc_engine e, int bone, const asc_bone_desc* des
       ASC_CUDA(cudaMalloc(&occ, grid));
       e->occ_cap[bone][j] = grid;
     }
-    build_occupancy(vh->dev, B.cut[j].lo, occ, nullptr);
+    build_occupancy(vh->dev, occupancy_threshold(B.cut[j]), occ, nullptr);
     B.occ[j] = occ;
   }
   ASC_CUDA(cudaStreamSynchronize(nullptr));
@@ -1675,6 +1736,7 @@ static int engine_launch(asc_engine e, int n, const int* bone, const double* man
   k_setup<<<1, 1024, 0, s>>>(e->dev, n, e->b, cost);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[1], s));
   k_ray<<<e->sms * e->launch.ray_blocks_per_sm, NRAY, 0, s>>>(e->dev, e->b, g_empty_skip, e->launch.ray_shape);
+  k_ray_fix<<<e->sms * 4, 128, 0, s>>>(e->dev, e->b, g_empty_skip);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[2], s));
   k_view<<<e->sms * e->view_grid(), VNT, e->smem, s>>>(e->dev, e->b, cost, vcost);
   if (e->host.cf_model) k_sad<<<e->sms * 8, 256, 0, s>>>(e->dev, e->b, cost, vcost);
@@ -1705,6 +1767,15 @@ ASC_API int asc_engine_stats(asc_engine e, float ms[3], unsigned long long* samp
   ASC_CUDA(cudaMemcpy(&C, e->b.C, sizeof C, cudaMemcpyDeviceToHost));
   if (samples) *samples = C.samples;
   if (pixels) *pixels = C.pixels;
+  return ASC_OK;
+}
+
+ASC_API int asc_engine_exact_rays(asc_engine e, int* n)
+{
+  if (!e || !n) return ASC_ERR_ARG;
+  Counters C;
+  ASC_CUDA(cudaMemcpy(&C, e->b.C, sizeof C, cudaMemcpyDeviceToHost));
+  *n = C.nfix;
   return ASC_OK;
 }
 

@@ -36,6 +36,7 @@ struct DevVolume {
   int px, pxy;            // padded row and slice pitch in voxels
   int storage;
   float norm;
+  float gmax;  // largest step between neighbouring stored voxels along an axis (raw units)
 };
 
 inline size_t padded_words(int nx, int ny, int nz, int storage)
@@ -65,6 +66,25 @@ inline void pack_pairs(int nx, int ny, int nz, int storage, F v, uint32_t* out)
           }
         }
       }
+}
+
+// The largest step between neighbouring voxels along an axis, max |v(p + e_i)
+// - v(p)|, of stored values v(x, y, z) (host side).  Bounds the slope of the
+// trilinear interpolant along every axis, so it turns a sample's position
+// error into a value error (Cutoff).  The clamp-to-edge apron adds no steps.
+template <class F>
+inline float volume_gmax(int nx, int ny, int nz, F v)
+{
+  float g = 0.f;
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x) {
+        const float a = v(x, y, z);
+        if (x + 1 < nx) g = std::max(g, std::fabs(v(x + 1, y, z) - a));
+        if (y + 1 < ny) g = std::max(g, std::fabs(v(x, y + 1, z) - a));
+        if (z + 1 < nz) g = std::max(g, std::fabs(v(x, y, z + 1) - a));
+      }
+  return g;
 }
 
 template <int STORE>
@@ -380,33 +400,70 @@ __device__ __host__ __forceinline__ void df_split(double d, float& h, float& l)
 }
 
 // The cutoff test of the march (RayCaster_kernels.cu:189: density += s >
-// cutoff ? step * s : 0), on raw voxel values.  An FP32 sample can differ
-// from the exact trilinear value of its exact position by up to ~1 raw unit
-// (sample positions carry ~5e-6 voxel of rounding; a step of 65535 between
-// neighbouring voxels turns that into 0.33 per axis), so a sample within
-// that much of the cutoff could fall on the other side of it than the exact
-// computation.  Samples in (lo, hi) are therefore decided again from their
-// double-float position and a double-float trilinear value against the
-// exact threshold c x vmax (c the normalized cutoff, vmax 65535 or 255: the
-// reference compares raw / vmax with c); all others are decided in FP32.
-// `raw` (c / norm) is the FP32 threshold of the occupancy grids, which are
-// built at `lo` so that every cell holding a voxel that a sample decided
-// exactly could count stays marched.
+// cutoff ? step * s : 0), on raw voxel values.  The reference compares
+// raw / vmax with c (vmax 65535 or 255); the exact threshold is c x vmax,
+// kept as the double-float (th, tl); the FP32 march compares with raw = c /
+// norm.
+//
+// An FP32 sample v differs from the exact trilinear value at its exact
+// position by at most
+//   u (3 |v| + 11 G)                   the seven lerps' roundings (the taps
+//                                      lie within 3 G of v)
+//   + G u (9 + 130 (|dX| + |dY| + |dZ|))  the position per axis: the
+//                                      fraction's rounding, the FMA of the
+//                                      sample offset (values below 1 + 64 |d|)
+//                                      and the offset times the dropped low
+//                                      part of d; the interpolant's slope
+//                                      along an axis is at most G
+// with u = 2^-24, G = DevVolume::gmax and d the per-sample step of each axis
+// in voxels; raw differs from c x vmax by at most 2 u |raw|.  So a sample
+// with |v - raw| >= t0 + t1 (|dX| + |dY| + |dZ|), t0 = u (7 |raw| + 24 G) +
+// 1e-6 and t1 = 140 u G, lies on the same side of the threshold in FP32 as
+// exactly (u |raw| of t0 covers the rounding of the band's ends).  The march decides such samples in FP32 and flags the rest (the
+// band); a flagged march is redone with the samples in the band decided from
+// their double-float position and a double-float trilinear value against
+// (th, tl) (sample_above).
+//
+// When |raw| <= 2 t0 the band is dropped (t0 = t1 = 0, the samples above
+// raw, i.e. at or above the next float hi0, counted): a sample decided the
+// other way then adds or leaves out at most |raw| + t0, a few times the FP32
+// error every counted sample carries, and a cutoff of 0 keeps its empty
+// cells (a band reaching below 0 would leave none).
+//
+// The occupancy grids are built at raw - t0 (<= c x vmax): a cell whose
+// voxels all lie at or below it holds only samples that the exact test
+// leaves out.
 struct Cutoff {
-  float raw, lo, hi;
-  float th, tl;  // c x vmax as a double-float
+  float raw;      // c / norm, the FP32 threshold
+  float hi0;      // raw, or with the band dropped the next float above it
+  float t0, t1;   // the band's half-width: t0 + t1 (|dX| + |dY| + |dZ|)
+  float th, tl;   // c x vmax as a double-float
 };
 
-__host__ __device__ inline Cutoff make_cutoff(float c, float norm)
+__host__ __device__ inline Cutoff make_cutoff(float c, float norm, float gmax)
 {
   Cutoff k;
   k.raw = c / norm;
-  const float tol = 1.0f + 1e-5f * fabsf(k.raw);
-  k.lo = k.raw - tol;
-  k.hi = k.raw + tol;
+  const float u = 5.9604645e-8f;  // 2^-24
+  k.t0 = u * (7.0f * fabsf(k.raw) + 24.0f * gmax) + 1e-6f;
+  k.t1 = 140.0f * u * gmax;
+  k.hi0 = k.raw;
+  if (!(fabsf(k.raw) > 2.0f * k.t0)) {
+    k.t0 = k.t1 = 0.f;
+    k.hi0 = nextafterf(k.raw, INFINITY);
+  }
   const double vmax = (double)(int)(1.0f / norm + 0.5f);
   df_split((double)c * vmax, k.th, k.tl);
   return k;
+}
+
+// The occupancy grids' threshold (Cutoff).
+__host__ __device__ inline float occupancy_threshold(const Cutoff& k) { return k.raw - k.t0; }
+
+// The band's half-width for a ray with per-sample steps dX, dY, dZ.
+__host__ __device__ inline float cutoff_band(const Cutoff& k, float dX, float dY, float dZ)
+{
+  return fmaf(k.t1, fabsf(dX) + fabsf(dY) + fabsf(dZ), k.t0);
 }
 
 // Per-ray set-up of cuda_volume_render_kernel (RayCaster_kernels.cu:144-186)
@@ -662,20 +719,15 @@ __device__ __forceinline__ void coord_base(df C, df dC, float k, int& base_i, fl
   frac = __fadd_rn(__fadd_rn(c.h, -fl), c.l);
 }
 
-// Whether sample k of a ray (texel coordinates X - k dX etc. as double-floats)
-// lies above the cutoff, computed exactly enough to agree with FP64: the
-// position and the trilinear value in double-float, against the threshold
-// (th, tl).  The rare slow path of the cutoff test (Cutoff); kept out of line
-// so that the march's registers do not pay for it.
+// Whether sample k of a ray lies above the cutoff, computed exactly enough
+// to agree with FP64: the position and the trilinear value in double-float,
+// against the threshold (th, tl) (Cutoff).  Decides the samples in the band.
 template <int STORE>
-__device__ __noinline__ bool sample_above(const DevVolume& V, float Xh, float Xl, float Yh, float Yl, float Zh,
-                                          float Zl, float dXh, float dXl, float dYh, float dYl, float dZh, float dZl,
-                                          int k, float th, float tl)
+__device__ __forceinline__ bool sample_above(const DevVolume& V, const RaySetup& r, int k, const Cutoff& cut)
 {
   const float kf = (float)k;
-  const df C[3] = {df_add(df{Xh, Xl}, df_neg(df_mulf(df{dXh, dXl}, kf))),
-                   df_add(df{Yh, Yl}, df_neg(df_mulf(df{dYh, dYl}, kf))),
-                   df_add(df{Zh, Zl}, df_neg(df_mulf(df{dZh, dZl}, kf)))};
+  const df C[3] = {df_add(r.X, df_neg(df_mulf(r.dX, kf))), df_add(r.Y, df_neg(df_mulf(r.dY, kf))),
+                   df_add(r.Z, df_neg(df_mulf(r.dZ, kf)))};
   int b[3];
   df f[3];
   for (int i = 0; i < 3; ++i) {
@@ -704,7 +756,7 @@ __device__ __noinline__ bool sample_above(const DevVolume& V, float Xh, float Xl
   const df f0 = df_add(e[0], df_mul(f[1], df_add(e[1], df_neg(e[0]))));
   const df f1 = df_add(e[2], df_mul(f[1], df_add(e[3], df_neg(e[2]))));
   const df v = df_add(f0, df_mul(f[2], df_add(f1, df_neg(f0))));
-  return df_lt(df{th, tl}, v);
+  return df_lt(df{cut.th, cut.tl}, v);
 }
 
 // Samples kb + js .. kb + je of one march block (kb a multiple of REBASE) of
@@ -714,7 +766,13 @@ __device__ __noinline__ bool sample_above(const DevVolume& V, float Xh, float Xl
 // 1e-7; the blocks are combined in double-float); a sample at or below the
 // cutoff leaves it untouched, so trimming samples that add nothing changes no
 // bit.
-template <int STORE>
+//
+// EXACT false: samples in the cutoff's band (Cutoff) are left out and mark
+// the block: the sum then comes back negated with its sign bit set (-0 for
+// an empty sum; a sum of samples above a cutoff >= 0 is never negative
+// otherwise, see block_flagged), and the ray must be marched again with
+// EXACT true, which decides those samples with sample_above.
+template <int STORE, bool EXACT>
 __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup& r, int kb, int js, int je,
                                               const Cutoff& cut)
 {
@@ -740,7 +798,22 @@ __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup&
                           ((unsigned)(bix + PAD) - BM);
   const unsigned imax = ASC_QUADS ? (unsigned)(V.nz + 2 * PAD - 1) * pxy - 1u
                                   : (unsigned)(V.nz + 2 * PAD - 1) * pxy - px - 1u;
+  // samples at or above hi count, samples in (lo, hi) are the band's
+  const float tol = cutoff_band(cut, dXh, dYh, dZh), lo = cut.raw - tol, hi = cut.hi0 + tol;
   float acc = 0.f;
+  bool near = false;
+  // the cutoff test of sample ks with value v: adds v when above
+  auto take = [&](float v, int ks) {
+    if (v >= hi) {
+      acc += v;
+    } else if (v > lo) {
+      if constexpr (EXACT) {
+        if (sample_above<STORE>(V, r, ks, cut)) acc += v;
+      } else {
+        near = true;
+      }
+    }
+  };
   float j = (float)js;
   // the taps' voxel index and weights of sample j (j * the low part of d
   // stays below 1e-6 voxel for j < REBASE)
@@ -751,22 +824,6 @@ __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup&
     ay = __fadd_rn(Y, -__fadd_rn(ty, -M));
     az = __fadd_rn(Z, -__fadd_rn(tz, -M));
     return min(__float_as_uint(tz) * pxy + __float_as_uint(ty) * px + __float_as_uint(tx) + i_base, imax);
-  };
-  // the exact cutoff test of sample ks (Cutoff), for values near the cutoff
-  auto exact = [&](int ks) {
-    return sample_above<STORE>(V, r.X.h, r.X.l, r.Y.h, r.Y.l, r.Z.h, r.Z.l, r.dX.h, r.dX.l, r.dY.h, r.dY.l, r.dZ.h,
-                               r.dZ.l, ks, cut.th, cut.tl);
-  };
-  // one sample's trilinear value from its taps, added when above the cutoff
-  auto accumulate = [&](const Taps<STORE>& t, float wx, float wy, float wz, int ks) {
-    const float e00 = lerp_tap<STORE>(t, 0, wx);
-    const float e10 = lerp_tap<STORE>(t, 1, wx);
-    const float e01 = lerp_tap<STORE>(t, 2, wx);
-    const float e11 = lerp_tap<STORE>(t, 3, wx);
-    const float f0 = fmaf(wy, e10 - e00, e00);
-    const float f1 = fmaf(wy, e11 - e01, e01);
-    const float v = fmaf(wz, f1 - f0, f0);
-    if (v > cut.lo && (v >= cut.hi || exact(ks))) acc += v;
   };
   // Samples two at a time (jj and jj + 1) in packed pairs, both samples'
   // loads issued together; the samples add in order.
@@ -789,17 +846,28 @@ __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup&
     locate2(j, wx, wy, wz, ia, ib);
     const Taps<STORE> A = fetch_taps<STORE>(P, ia, px, pxy), B = fetch_taps<STORE>(P, ib, px, pxy);
     const float2 v = trilinear2<STORE>(A, B, wx, wy, wz);
-    if (v.x > cut.lo && (v.x >= cut.hi || exact(kb + k))) acc += v.x;
-    if (v.y > cut.lo && (v.y >= cut.hi || exact(kb + k + 1))) acc += v.y;
+    take(v.x, kb + k);
+    take(v.y, kb + k + 1);
     j += 2.0f;
   }
   if (k == je) {
     float ax, ay, az;
-    const Taps<STORE> A = fetch_taps<STORE>(P, locate(j, ax, ay, az), px, pxy);
-    accumulate(A, ax, ay, az, kb + k);
+    const Taps<STORE> t = fetch_taps<STORE>(P, locate(j, ax, ay, az), px, pxy);
+    const float e00 = lerp_tap<STORE>(t, 0, ax);
+    const float e10 = lerp_tap<STORE>(t, 1, ax);
+    const float e01 = lerp_tap<STORE>(t, 2, ax);
+    const float e11 = lerp_tap<STORE>(t, 3, ax);
+    const float f0 = fmaf(ay, e10 - e00, e00);
+    const float f1 = fmaf(ay, e11 - e01, e01);
+    const float v = fmaf(az, f1 - f0, f0);
+    take(v, kb + k);
   }
-  return acc;
+  if constexpr (EXACT) return acc;
+  return near ? -acc - 0.0f : acc;
 }
+
+// Whether a march block's sum carries the band's mark (march_block).
+__device__ __forceinline__ bool block_flagged(float p) { return (__float_as_uint(p) >> 31) != 0u; }
 
 // Adds a block's sum to the ray's double-float total; blocks that added
 // nothing leave it untouched.
@@ -808,27 +876,46 @@ __device__ __forceinline__ void add_block(df& total, float p)
   if (p != 0.f) total = df_add(total, df{p, 0.f});
 }
 
-// One whole ray: the march blocks that hold occupied samples, in order, each
-// trimmed to its occupied extent, their sums combined in double-float.  The
-// result depends only on the samples above the cutoff, so it is the same
-// with and without `occ`, and the same as the batched engine's.
+// One march pass over a whole ray: the march blocks that hold occupied
+// samples, in order, each trimmed to its occupied extent, their sums combined
+// in double-float.  EXACT false: *flagged is set when a sample fell in the
+// cutoff's band (the pass's total then leaves the band's samples out).
+template <int STORE, bool EXACT>
+__device__ __forceinline__ float march_pass(const DevVolume& V, const uint8_t* __restrict__ occ, const RaySetup& r,
+                                            const Cutoff& cut, bool* flagged)
+{
+  CellWalk w = cell_walk(V, r, 0);
+  WalkState s{0, r.K - 1, 0, -1, 0};
+  const RayTrim t = ray_trim(V, r);
+  df total{0.f, 0.f};
+  bool fl = false;
+  walk_segments(w, occ, [&](int i, float& ia, float& c) {
+    ia = t.ia[i];
+    c = t.c[i];
+  }, s, [&](int kb, int js, int je) {
+    const float p = march_block<STORE, EXACT>(V, r, kb, js, je, cut);
+    if (!EXACT && block_flagged(p))
+      fl = true;
+    else
+      add_block(total, p);
+    return true;
+  });
+  if (flagged) *flagged = fl;
+  return total.h + total.l;
+}
+
+// One whole ray, with every cutoff decision the exact one: the FP32 pass,
+// and the exact pass when a sample fell in the band.  The result depends
+// only on the samples above the cutoff, so it is the same with and without
+// `occ`, and the same as the batched engine's.
 template <int STORE>
 __device__ __forceinline__ float march(const DevVolume& V, const uint8_t* __restrict__ occ, const RaySetup& r,
                                        const Cutoff& cut)
 {
   if (r.K <= 0) return 0.f;
-  CellWalk w = cell_walk(V, r, 0);
-  WalkState s{0, r.K - 1, 0, -1, 0};
-  const RayTrim t = ray_trim(V, r);
-  df total{0.f, 0.f};
-  walk_segments(w, occ, [&](int i, float& ia, float& c) {
-    ia = t.ia[i];
-    c = t.c[i];
-  }, s, [&](int kb, int js, int je) {
-    add_block(total, march_block<STORE>(V, r, kb, js, je, cut));
-    return true;
-  });
-  return total.h + total.l;
+  bool flagged = false;
+  const float d = march_pass<STORE, false>(V, occ, r, cut, &flagged);
+  return flagged ? march_pass<STORE, true>(V, occ, r, cut, nullptr) : d;
 }
 
 }  // namespace asc

@@ -793,7 +793,19 @@ ASC_API int asc_volume_create(const void* data, int W, int H, int D, int bps, co
     return cuda_status(e);
   }
   const int px = dims[0] + 2 * PAD, pxy = px * (dims[1] + 2 * PAD);
-  v->dev = DevVolume{v->pairs, dims[0], dims[1], dims[2], px, pxy, storage, 1.0f / norm};
+  // the stored values' largest neighbour step (the march's cutoff band)
+  const float gmax = volume_gmax(dims[0], dims[1], dims[2], [&](int x, int y, int z) {
+    const uint32_t w = to_store(vals[(size_t)z * dxy + (size_t)y * dx + x], storage);
+    if (storage == ASC_STORE_F16) return __half2float(__ushort_as_half((unsigned short)w));
+    if (storage == ASC_STORE_BF16) return __bfloat162float(__ushort_as_bfloat16((unsigned short)w));
+    if (storage == ASC_STORE_F32) {
+      float f;
+      memcpy(&f, &w, 4);
+      return f;
+    }
+    return (float)w;
+  });
+  v->dev = DevVolume{v->pairs, dims[0], dims[1], dims[2], px, pxy, storage, 1.0f / norm, gmax};
   *out = (asc_volume)v;
   return ASC_OK;
 }
@@ -835,7 +847,7 @@ int raycast_launch(const DevVolume& V, const uint8_t* occ, const float* m12, con
   a.step = step;
   // density = step * sum(norm * raw) / intensity; cutoff compares normalized samples
   a.scale = step * V.norm / intensity;
-  a.cut = make_cutoff(cutoff, V.norm);
+  a.cut = make_cutoff(cutoff, V.norm, V.gmax);
   df_split((double)vp[2] / (double)w, a.sx[0], a.sx[1]);
   df_split((double)vp[3] / (double)h, a.sy[0], a.sy[1]);
   dim3 grid((w + 15) / 16, (h + 15) / 16);
@@ -867,7 +879,7 @@ ASC_API int asc_raycast(asc_volume vol, const double imv[16], const float vp[4],
   fold_matrix(imv, v->inv_scale, v->inv_trans, m);
   const uint8_t* occ = nullptr;
   if (g_empty_skip) {
-    const float cut = make_cutoff(cutoff, v->dev.norm).lo;  // the occupancy grid's threshold
+    const float cut = occupancy_threshold(make_cutoff(cutoff, v->dev.norm, v->dev.gmax));
     if (!v->occ) {
       Gate g(device_gate());
       ASC_CUDA(cudaMalloc(&v->occ, occ_grid_bytes(occupancy_cells(v->dev))));

@@ -376,6 +376,8 @@ def main():
     cnt = (C.c_ulonglong * 4)()
     L.call("asc_engine_counters", eng.handle, cnt)
     marched, slots = cnt[2], cnt[3]
+    nexact = C.c_int()
+    L.call("asc_engine_exact_rays", eng.handle, C.byref(nexact))
     rl = roofline(phase, samples.value, pixels.value, marched, slots, clk.summary().get("sm_mhz"))
     # ---- plain per-pose drop-in form on the same GPU (sampled)
     plain_v = None
@@ -398,14 +400,15 @@ def main():
                 "vs_baseline": None, "dtype": "f32 (u16 volumes, FP64 pose/NCC combine)", "data": "synthetic",
                 "config": dict(CONFIG, l2="256 MB memset between timed steps", parallelism=f"replicas x{ws}"),
                 "e2e": {"value": e2e, "unit": "pose-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-                # per step: k_pso_init, then per iteration one graph of six kernels
-                # (k_pso_update, k_setup_iv, k_setup, k_ray, k_view, k_pso_best)
-                "gpu_launches": args.steps * (1 + 6 * iters),
+                # per step: k_pso_init, then per iteration one graph of seven kernels
+                # (k_pso_update, k_setup_iv, k_setup, k_ray, k_ray_fix, k_view, k_pso_best)
+                "gpu_launches": args.steps * (1 + 7 * iters),
                 "roofline": rl,
                 "kernel_ms": {"setup": phase[0], "ray": phase[1], "view": phase[2]},
                 "launch": launch,
                 "work": {"samples_per_batch": samples.value, "marched_per_batch": marched,
-                         "pixels_per_batch": pixels.value, "batch": nb * npart},
+                         "pixels_per_batch": pixels.value, "batch": nb * npart,
+                         "exact_cutoff_rays_per_batch": nexact.value},
                 "plain": {"value": plain_v, "unit": "pose-evals/s",
                           "speedup": value / plain_v if plain_v else None},
                 "cpu_baseline": cpu, "clocks": clk.summary(),
@@ -679,10 +682,12 @@ def run_roofline(args):
         ms.append(list(t3))
     cnt = (C.c_ulonglong * 4)()
     L.call("asc_engine_counters", eng.handle, cnt)
+    nexact = C.c_int()
+    L.call("asc_engine_exact_rays", eng.handle, C.byref(nexact))
     ms = np.array(ms)
     return {"workload": "roofline batch", "storage": args.storage, "items": nb * npart, "views": 2, "reps": args.reps,
             "samples_per_launch": cnt[0], "pixels_per_launch": cnt[1], "marched_per_launch": cnt[2],
-            "lane_slots_per_launch": cnt[3], "setup_ms": float(ms[:, 0].mean()), "ray_ms": float(ms[:, 1].mean()),
+            "lane_slots_per_launch": cnt[3], "exact_cutoff_rays_per_launch": nexact.value, "setup_ms": float(ms[:, 0].mean()), "ray_ms": float(ms[:, 1].mean()),
             "view_ms": float(ms[:, 2].mean())}
 
 

@@ -320,6 +320,12 @@ int asc_engine_stats(asc_engine e, float ms[3], unsigned long long *samples, uns
  * slots the marching warps occupied (32 x the longest marched span of each
  * warp's rays); out[2] / out[3] is the SIMT efficiency of the march. */
 int asc_engine_counters(asc_engine e, unsigned long long out[4]);
+/* Rays of the last evaluation that the ray cast marched a second time: rays
+ * with a sample whose FP32 value lay within rounding of the cutoff, whose
+ * decision (RayCaster_kernels.cu:190, sample > cutoff) was then made from a
+ * double-float position and value, so that every DRR pixel counts the same
+ * samples as an exact computation.  No counterpart in the reference. */
+int asc_engine_exact_rays(asc_engine e, int *n);
 
 /* ---- device-resident optimizers ----
  * Synchronous batched PSO over all bones at once: n_particles per bone,

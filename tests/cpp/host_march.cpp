@@ -35,8 +35,14 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
     return (uint32_t)(storage == ASC_STORE_BF16 ? to_bf16(v) : v);
   }, pairs.data());
   const int px = nx + 2 * PAD, pxy = px * (ny + 2 * PAD);
-  DevVolume V{pairs.data(), nx, ny, nz, px, pxy, storage, 1.0f / 65535.0f};
-  const Cutoff cut = make_cutoff(cutoff, V.norm);
+  DevVolume V{pairs.data(), nx, ny, nz, px, pxy, storage, 1.0f / 65535.0f, 0.f};
+  V.gmax = volume_gmax(nx, ny, nz, [&](int x, int y, int z) {
+    const size_t i = (size_t)(z + PAD) * pxy + (size_t)(y + PAD) * px + (x + PAD);
+    return storage == ASC_STORE_BF16  ? voxel_value<ASC_STORE_BF16>(V, i)
+           : storage == ASC_STORE_F32 ? voxel_value<ASC_STORE_F32>(V, i)
+                                      : voxel_value<ASC_STORE_U16>(V, i);
+  });
+  const Cutoff cut = make_cutoff(cutoff, V.norm, V.gmax);
   // occupancy as k_occupancy builds it
   const int bx = occ_dim(nx), by = occ_dim(ny), bz = occ_dim(nz);
   const size_t ncell = (size_t)bx * by * bz;
@@ -47,7 +53,7 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
       for (int cx = -OCC_PAD; cx < bx - OCC_PAD; ++cx) {
         const size_t c = ((size_t)(cz + OCC_PAD) * by + (cy + OCC_PAD)) * bx + (cx + OCC_PAD);
         int box[4];
-        o8[c] = occ_cell(cx, cy, cz, nx, ny, nz, cut.lo, [&](int x, int y, int z) {
+        o8[c] = occ_cell(cx, cy, cz, nx, ny, nz, occupancy_threshold(cut), [&](int x, int y, int z) {
           const size_t i = (size_t)(z + PAD) * pxy + (size_t)(y + PAD) * px + (x + PAD);
           return storage == ASC_STORE_BF16  ? voxel_value<ASC_STORE_BF16>(V, i)
                  : storage == ASC_STORE_F32 ? voxel_value<ASC_STORE_F32>(V, i)
@@ -82,7 +88,9 @@ extern "C" int hm_raycast(const uint16_t* vol, int nx, int ny, int nz, int stora
 // box, 2 box covering the cell).
 extern "C" void hm_occupancy(const uint16_t* vol, int nx, int ny, int nz, float cutoff, long long* counts)
 {
-  const float cut = make_cutoff(cutoff, 1.0f / 65535.0f).lo;  // the grids' threshold, as the library builds them
+  const float g = volume_gmax(nx, ny, nz, [&](int x, int y, int z) { return (float)vol[((size_t)z * ny + y) * nx + x]; });
+  // the grids' threshold, as the library builds them
+  const float cut = occupancy_threshold(make_cutoff(cutoff, 1.0f / 65535.0f, g));
   const int bx = occ_dim(nx), by = occ_dim(ny), bz = occ_dim(nz);
   counts[0] = counts[1] = counts[2] = 0;
   for (int cz = -OCC_PAD; cz < bz - OCC_PAD; ++cz)

@@ -198,8 +198,10 @@ def test_cutoff_at_a_voxel_level_decides_as_fp64():
     alone would round to the level itself): the plain ray caster and the
     batched engine count every sample of the uniform 200 soft tissue, as the
     FP64 oracle does (RayCaster_kernels.cu:189), and the engine's costs stay
-    within the NCC bar."""
-    sc = S.make_scene([(40, 36, 44)], 1.0, (96, 96), 1.0, filters="sobel", seed=4)
+    within the NCC bar.  No filters: on a noise-free phantom a Sobel image is
+    exactly 0 over flat regions in FP64 but ~1e-9 in FP32, which moves the
+    DRR mask (Tracker.cpp:722-735) by whole pixels, whatever the march does."""
+    sc = S.make_scene([(40, 36, 44)], 1.0, (96, 96), 1.0, filters="none", seed=4)
     sc.volumes[0].data = S.phantom((40, 36, 44), seed=4, noise=0.0)
     cut = float(np.float32(200.0 / 65535.0))
     for row in sc.ray:
