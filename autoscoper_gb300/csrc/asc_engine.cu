@@ -9,8 +9,8 @@
 //   k_ray         persistent: 16x16-ray tiles pulled from an atomic queue,
 //                            DRRs written to a packed buffer; rays with a
 //                            sample within rounding of the cutoff are listed;
-//   k_ray_fix     grid-stride: the listed rays marched again with exact
-//                            cutoff decisions;
+//   k_ray_fix     a warp per listed tile: its marked rays marched again
+//                            with exact cutoff decisions;
 //   k_view        persistent: 48x48 output tiles pulled from a queue; each
 //                            stages DRR and radiograph regions with the chain's
 //                            halo in shared memory, runs both filter chains,
@@ -329,8 +329,9 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
 // single ray.  A ray with more than NBW segments takes further passes.
 template <int STORE>
 __device__ __forceinline__ void march_segments(const DevVolume& V, const float4 (*rec)[NRAY], const unsigned* ord,
-                                               float* part, int nseg, int* grab, const Cutoff& cut,
-                                               unsigned long long& marched, unsigned long long& slots)
+                                               float* part, int nseg, int* grab, const float4* band,
+                                               const Cutoff& cut, unsigned long long& marched,
+                                               unsigned long long& slots)
 {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -353,7 +354,10 @@ __device__ __forceinline__ void march_segments(const DevVolume& V, const float4 
       r.dY = df{q2.x, q2.y};
       r.dZ = df{q2.z, q2.w};
       const int kb = __float_as_int(part[slot]);  // the block start, until the sum replaces it
-      part[slot] = march_block<STORE, false>(V, r, kb, js, je, cut);
+      // this ray's band: the tile's raw - t0, hi0 + t0 and t1 (cutoff_bounds)
+      const float4 c = *band;
+      const float S = fabsf(q1.z) + fabsf(q2.x) + fabsf(q2.z);
+      part[slot] = march_block<STORE, false>(V, r, kb, js, je, fmaf(-c.z, S, c.x), fmaf(c.z, S, c.y), cut);
       len = je - js + 1;
     }
     const unsigned tot = __reduce_add_sync(FULL, (unsigned)len), mx = __reduce_max_sync(FULL, (unsigned)len);
@@ -377,16 +381,31 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
   __shared__ unsigned s_ord[NRAY * NBW]; // the segments, longest first
   __shared__ int s_cnt[REBASE];          // segments per length - 1, then placement cursors
   __shared__ int s_tile, s_nseg, s_grab, s_k;
+  __shared__ float4 s_band;              // the tile's cutoff: raw - t0, hi0 + t0, t1
+  __shared__ int s_fix;                  // 1 + the last tile, when one of its rays was marked
   const unsigned FULL = 0xffffffffu;
   const int tid = threadIdx.x, lane = tid & 31;
   unsigned long long marched = 0, slots = 0, sampled = 0;
+  if (tid == 0) s_fix = 0;
   for (;;) {
     if (tid == 0) {
       const int tl = atomicAdd(&b.C->rnext, 1);
       s_tile = tl;
-      s_k = tl < b.C->rtiles ? find_iv(b.roff, b.C->n_iv, tl) : 0;
+      int kk = 0;
+      if (tl < b.C->rtiles) {
+        kk = find_iv(b.roff, b.C->n_iv, tl);
+        const IV& q = b.iv[kk];
+        const Cutoff& c = sc->bones[q.bone].cut[q.slot];
+        s_band = make_float4(c.raw - c.t0, c.hi0 + c.t0, c.t1, 0.f);
+      }
+      s_k = kk;
     }
     __syncthreads();
+    // the last tile's mark (set after its last barrier, visible past this one)
+    if (tid == 0 && s_fix) {
+      b.fixt[atomicAdd(&b.C->nfixt, 1)] = s_fix - 1;
+      s_fix = 0;
+    }
     const int tile = s_tile;
     if (tile >= b.C->rtiles) break;
     const int k = s_k;
@@ -424,8 +443,7 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
       done = false;
     }
     WalkState ws{0, rs.K - 1, 0, -1, 0};
-    df total{0.f, 0.f};
-    bool flagged = false;
+    df total{0.f, 0.f};  // NaN once a segment met the cutoff's band
     for (;;) {
       if (tid < REBASE) s_cnt[tid] = 0;
       if (tid == 0) s_grab = 0;
@@ -469,30 +487,34 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
       const int nseg = s_nseg;
       // ---- march the segments, 32 at a time per warp
       if (B.vol.storage == ASC_STORE_F32)
-        march_segments<ASC_STORE_F32>(B.vol, s_rec, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
+        march_segments<ASC_STORE_F32>(B.vol, s_rec, s_ord, s_part, nseg, &s_grab, &s_band, cut, marched,
+                                      slots);
       else if (B.vol.storage == ASC_STORE_BF16)
-        march_segments<ASC_STORE_BF16>(B.vol, s_rec, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
+        march_segments<ASC_STORE_BF16>(B.vol, s_rec, s_ord, s_part, nseg, &s_grab, &s_band, cut, marched,
+                                      slots);
       else if (B.vol.storage == ASC_STORE_F16)
-        march_segments<ASC_STORE_F16>(B.vol, s_rec, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
+        march_segments<ASC_STORE_F16>(B.vol, s_rec, s_ord, s_part, nseg, &s_grab, &s_band, cut, marched,
+                                      slots);
       else
-        march_segments<ASC_STORE_U16>(B.vol, s_rec, s_ord, s_part, nseg, &s_grab, cut, marched, slots);
+        march_segments<ASC_STORE_U16>(B.vol, s_rec, s_ord, s_part, nseg, &s_grab, &s_band, cut, marched,
+                                      slots);
       __syncthreads();
       // ---- this ray's segments, in order
       for (int i = 0; i < n; ++i) {
         const float p = s_part[tid * NBW + i];
         if (block_flagged(p))
-          flagged = true;
+          total.h = __int_as_float(0x7fffffff);  // NaN stays NaN through add_block
         else
           add_block(total, p);
       }
       if (!__syncthreads_or(!done)) break;
     }
-    const bool fix = valid && flagged;
-    if (valid)
-      b.drr[r.pix + (long long)y * r.w + x] = fix ? -1.0f : fminf(fmaxf((total.h + total.l) * B.scale[j], 0.f), 1.f);
-    const unsigned fm = __ballot_sync(FULL, fix);
-    if (lane == 0 && fm) atomicAdd(&b.C->nfix, __popc(fm));
-    if (__syncthreads_or(fix) && tid == 0) b.fixt[atomicAdd(&b.C->nfixt, 1)] = tile;
+    if (valid) {
+      const bool flagged = total.h != total.h;
+      b.drr[r.pix + (long long)y * r.w + x] =
+          flagged ? -1.0f : fminf(fmaxf((total.h + total.l) * B.scale[j], 0.f), 1.f);
+      if (flagged) s_fix = tile + 1;
+    }
   }
   if (lane == 0 && sampled) atomicAdd(&b.C->samples, sampled);
   if (lane == 0 && slots) {
@@ -503,38 +525,54 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
 
 // The marked rays of the tiles on the fix list, marched again with every
 // cutoff decision the exact one (march_pass with EXACT); each overwrites its
-// mark.  A thread per (listed tile, ray); the ray set-up is k_ray's, so the
-// samples are the same.
-__global__ void __launch_bounds__(128) k_ray_fix(const SceneDev* __restrict__ sc, Bufs b, int skip)
+// mark.  A warp per listed tile: its marked rays, found by ballots over the
+// tile's 256 pixels, are dealt to the lanes, so a tile's rays march side by
+// side.  The ray set-up is k_ray's, so the samples are the same.
+constexpr int FIX_THREADS = 128;
+__global__ void __launch_bounds__(FIX_THREADS) k_ray_fix(const SceneDev* __restrict__ sc, Bufs b, int skip)
 {
-  const long long n = (long long)b.C->nfixt * NRAY;
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-    const int tile = b.fixt[q / NRAY], p = (int)(q % NRAY);
+  __shared__ unsigned char s_pix[FIX_THREADS / 32][NRAY];  // per warp: the tile's marked rays
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int nt = b.C->nfixt;
+  const int nw = gridDim.x * (FIX_THREADS / 32);
+  for (int w = blockIdx.x * (FIX_THREADS / 32) + wib; w < nt; w += nw) {
+    const int tile = b.fixt[w];
     const int k = find_iv(b.roff, b.C->n_iv, tile);
     const IV& r = b.iv[k];
     const int t = tile - b.roff[k];
-    const int x = (t % r.rtx) * RTX + (p % RTX), y = (t / r.rtx) * RTY + p / RTX;
-    if (x >= r.w || y >= r.h) continue;
-    float* px = b.drr + r.pix + (long long)y * r.w + x;
-    if (!(*px < 0.f)) continue;
+    const int x0 = (t % r.rtx) * RTX, y0 = (t / r.rtx) * RTY;
+    int cnt = 0;
+    for (int c = 0; c < NRAY / 32; ++c) {
+      const int p = c * 32 + lane, x = x0 + p % RTX, y = y0 + p / RTX;
+      const bool marked = x < r.w && y < r.h && b.drr[r.pix + (long long)y * r.w + x] < 0.f;
+      const unsigned m = __ballot_sync(0xffffffffu, marked);
+      if (marked) s_pix[wib][cnt + __popc(m & ((1u << lane) - 1u))] = (unsigned char)p;
+      cnt += __popc(m);
+    }
+    __syncwarp();
+    if (lane == 0) atomicAdd(&b.C->nfix, cnt);
     const BoneDev& B = sc->bones[r.bone];
     const int j = r.slot;
-    RaySetup rs;
-    float d = 0.f;
-    if (ray_setup(r.m, r.vp, x, y, df{r.sx[0], r.sx[1]}, df{r.sy[0], r.sy[1]}, B.step[j], B.vol.nx, B.vol.ny,
-                  B.vol.nz, rs) &&
-        rs.K > 0) {
-      const uint8_t* occ = skip ? B.occ[j] : nullptr;
-      if (B.vol.storage == ASC_STORE_F32)
-        d = march_pass<ASC_STORE_F32, true>(B.vol, occ, rs, B.cut[j], nullptr);
-      else if (B.vol.storage == ASC_STORE_BF16)
-        d = march_pass<ASC_STORE_BF16, true>(B.vol, occ, rs, B.cut[j], nullptr);
-      else if (B.vol.storage == ASC_STORE_F16)
-        d = march_pass<ASC_STORE_F16, true>(B.vol, occ, rs, B.cut[j], nullptr);
-      else
-        d = march_pass<ASC_STORE_U16, true>(B.vol, occ, rs, B.cut[j], nullptr);
+    const uint8_t* occ = skip ? B.occ[j] : nullptr;
+    for (int i = lane; i < cnt; i += 32) {
+      const int p = s_pix[wib][i], x = x0 + p % RTX, y = y0 + p / RTX;
+      RaySetup rs;
+      float d = 0.f;
+      if (ray_setup(r.m, r.vp, x, y, df{r.sx[0], r.sx[1]}, df{r.sy[0], r.sy[1]}, B.step[j], B.vol.nx, B.vol.ny,
+                    B.vol.nz, rs) &&
+          rs.K > 0) {
+        if (B.vol.storage == ASC_STORE_F32)
+          d = march_pass<ASC_STORE_F32, true>(B.vol, occ, rs, B.cut[j], nullptr);
+        else if (B.vol.storage == ASC_STORE_BF16)
+          d = march_pass<ASC_STORE_BF16, true>(B.vol, occ, rs, B.cut[j], nullptr);
+        else if (B.vol.storage == ASC_STORE_F16)
+          d = march_pass<ASC_STORE_F16, true>(B.vol, occ, rs, B.cut[j], nullptr);
+        else
+          d = march_pass<ASC_STORE_U16, true>(B.vol, occ, rs, B.cut[j], nullptr);
+      }
+      b.drr[r.pix + (long long)y * r.w + x] = fminf(fmaxf(d * B.scale[j], 0.f), 1.f);
     }
-    *px = fminf(fmaxf(d * B.scale[j], 0.f), 1.f);
+    __syncwarp();
   }
 }
 
@@ -1736,7 +1774,7 @@ static int engine_launch(asc_engine e, int n, const int* bone, const double* man
   k_setup<<<1, 1024, 0, s>>>(e->dev, n, e->b, cost);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[1], s));
   k_ray<<<e->sms * e->launch.ray_blocks_per_sm, NRAY, 0, s>>>(e->dev, e->b, g_empty_skip, e->launch.ray_shape);
-  k_ray_fix<<<e->sms * 4, 128, 0, s>>>(e->dev, e->b, g_empty_skip);
+  k_ray_fix<<<e->sms * 4, FIX_THREADS, 0, s>>>(e->dev, e->b, g_empty_skip);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[2], s));
   k_view<<<e->sms * e->view_grid(), VNT, e->smem, s>>>(e->dev, e->b, cost, vcost);
   if (e->host.cf_model) k_sad<<<e->sms * 8, 256, 0, s>>>(e->dev, e->b, cost, vcost);

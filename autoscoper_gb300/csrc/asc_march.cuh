@@ -417,12 +417,13 @@ __device__ __host__ __forceinline__ void df_split(double d, float& h, float& l)
 //                                      along an axis is at most G
 // with u = 2^-24, G = DevVolume::gmax and d the per-sample step of each axis
 // in voxels; raw differs from c x vmax by at most 2 u |raw|.  So a sample
-// with |v - raw| >= t0 + t1 (|dX| + |dY| + |dZ|), t0 = u (7 |raw| + 24 G) +
+// with |v - raw| >= t0 + t1 (|dX| + |dY| + |dZ|), t0 = u (8 |raw| + 24 G) +
 // 1e-6 and t1 = 140 u G, lies on the same side of the threshold in FP32 as
-// exactly (u |raw| of t0 covers the rounding of the band's ends).  The march decides such samples in FP32 and flags the rest (the
-// band); a flagged march is redone with the samples in the band decided from
-// their double-float position and a double-float trilinear value against
-// (th, tl) (sample_above).
+// exactly (3 u |raw| of t0 cover the roundings of the band's ends).  The
+// march decides such samples in FP32 and flags the rest (the band); a
+// flagged march is redone with the samples in the band decided from their
+// double-float position and a double-float trilinear value against (th, tl)
+// (sample_above).
 //
 // When |raw| <= 2 t0 the band is dropped (t0 = t1 = 0, the samples above
 // raw, i.e. at or above the next float hi0, counted): a sample decided the
@@ -445,7 +446,7 @@ __host__ __device__ inline Cutoff make_cutoff(float c, float norm, float gmax)
   Cutoff k;
   k.raw = c / norm;
   const float u = 5.9604645e-8f;  // 2^-24
-  k.t0 = u * (7.0f * fabsf(k.raw) + 24.0f * gmax) + 1e-6f;
+  k.t0 = u * (8.0f * fabsf(k.raw) + 24.0f * gmax) + 1e-6f;
   k.t1 = 140.0f * u * gmax;
   k.hi0 = k.raw;
   if (!(fabsf(k.raw) > 2.0f * k.t0)) {
@@ -460,10 +461,13 @@ __host__ __device__ inline Cutoff make_cutoff(float c, float norm, float gmax)
 // The occupancy grids' threshold (Cutoff).
 __host__ __device__ inline float occupancy_threshold(const Cutoff& k) { return k.raw - k.t0; }
 
-// The band's half-width for a ray with per-sample steps dX, dY, dZ.
-__host__ __device__ inline float cutoff_band(const Cutoff& k, float dX, float dY, float dZ)
+// The band of a ray with per-sample steps dX, dY, dZ: samples in (lo, hi)
+// are decided exactly, samples at or above hi count.
+__host__ __device__ inline void cutoff_bounds(const Cutoff& k, float dX, float dY, float dZ, float& lo, float& hi)
 {
-  return fmaf(k.t1, fabsf(dX) + fabsf(dY) + fabsf(dZ), k.t0);
+  const float tol = fmaf(k.t1, fabsf(dX) + fabsf(dY) + fabsf(dZ), k.t0);
+  lo = k.raw - tol;
+  hi = k.hi0 + tol;
 }
 
 // Per-ray set-up of cuda_volume_render_kernel (RayCaster_kernels.cu:144-186)
@@ -767,14 +771,16 @@ __device__ __forceinline__ bool sample_above(const DevVolume& V, const RaySetup&
 // cutoff leaves it untouched, so trimming samples that add nothing changes no
 // bit.
 //
-// EXACT false: samples in the cutoff's band (Cutoff) are left out and mark
-// the block: the sum then comes back negated with its sign bit set (-0 for
-// an empty sum; a sum of samples above a cutoff >= 0 is never negative
-// otherwise, see block_flagged), and the ray must be marched again with
-// EXACT true, which decides those samples with sample_above.
+// lo, hi: the cutoff's band for this ray (cutoff_bounds): samples at or
+// above hi count, samples in (lo, hi) need the exact test.  EXACT false: a
+// sample in the band marks the block, whose sum then comes back negated with
+// its sign bit set (-0 for an empty sum; a sum of samples above a cutoff >= 0
+// is never negative otherwise, see block_flagged), and the ray must be
+// marched again with EXACT true, which decides those samples with
+// sample_above.  cut is read only with EXACT.
 template <int STORE, bool EXACT>
 __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup& r, int kb, int js, int je,
-                                              const Cutoff& cut)
+                                              float lo, float hi, const Cutoff& cut)
 {
   const uint32_t* __restrict__ P = V.pairs;
   const unsigned px = (unsigned)V.px, pxy = (unsigned)V.pxy;
@@ -798,20 +804,21 @@ __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup&
                           ((unsigned)(bix + PAD) - BM);
   const unsigned imax = ASC_QUADS ? (unsigned)(V.nz + 2 * PAD - 1) * pxy - 1u
                                   : (unsigned)(V.nz + 2 * PAD - 1) * pxy - px - 1u;
-  // samples at or above hi count, samples in (lo, hi) are the band's
-  const float tol = cutoff_band(cut, dXh, dYh, dZh), lo = cut.raw - tol, hi = cut.hi0 + tol;
   float acc = 0.f;
-  bool near = false;
+  // > 0 once a sample fell in (lo, hi): min(v - lo, hi - v) > 0 exactly then
+  // (the sign of a rounded difference is the exact one)
+  float nearf = -1.0f;
   // the cutoff test of sample ks with value v: adds v when above
   auto take = [&](float v, int ks) {
-    if (v >= hi) {
-      acc += v;
-    } else if (v > lo) {
-      if constexpr (EXACT) {
+    if constexpr (EXACT) {
+      if (v >= hi) {
+        acc += v;
+      } else if (v > lo) {
         if (sample_above<STORE>(V, r, ks, cut)) acc += v;
-      } else {
-        near = true;
       }
+    } else {
+      acc += v >= hi ? v : 0.0f;
+      nearf = fmaxf(nearf, fminf(v - lo, hi - v));
     }
   };
   float j = (float)js;
@@ -826,12 +833,14 @@ __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup&
     return min(__float_as_uint(tz) * pxy + __float_as_uint(ty) * px + __float_as_uint(tx) + i_base, imax);
   };
   // Samples two at a time (jj and jj + 1) in packed pairs, both samples'
-  // loads issued together; the samples add in order.
-  const float2 dX2 = bcast2(-dXh), dY2 = bcast2(-dYh), dZ2 = bcast2(-dZh);
-  const float2 fx2 = bcast2(fx), fy2 = bcast2(fy), fz2 = bcast2(fz);
+  // loads issued together; the samples add in order.  The positions are
+  // scalar FMAs (the same values as locate's): packed ones would hold six
+  // more registers, which the march, at 64 per thread, spills.
   auto locate2 = [&](float jj, float2& wx, float2& wy, float2& wz, unsigned& ia, unsigned& ib) {
-    const float2 J = make_float2(jj, jj + 1.0f);
-    const float2 X = __ffma2_rn(J, dX2, fx2), Y = __ffma2_rn(J, dY2, fy2), Z = __ffma2_rn(J, dZ2, fz2);
+    const float j1 = jj + 1.0f;
+    const float2 X = make_float2(fmaf(-jj, dXh, fx), fmaf(-j1, dXh, fx));
+    const float2 Y = make_float2(fmaf(-jj, dYh, fy), fmaf(-j1, dYh, fy));
+    const float2 Z = make_float2(fmaf(-jj, dZh, fz), fmaf(-j1, dZh, fz));
     const float2 tx = __fadd2_rd(X, bcast2(M)), ty = __fadd2_rd(Y, bcast2(M)), tz = __fadd2_rd(Z, bcast2(M));
     wx = sub2(X, __fadd2_rn(tx, bcast2(-M)));
     wy = sub2(Y, __fadd2_rn(ty, bcast2(-M)));
@@ -863,7 +872,7 @@ __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup&
     take(v, kb + k);
   }
   if constexpr (EXACT) return acc;
-  return near ? -acc - 0.0f : acc;
+  return nearf > 0.0f ? -acc - 0.0f : acc;
 }
 
 // Whether a march block's sum carries the band's mark (march_block).
@@ -889,11 +898,13 @@ __device__ __forceinline__ float march_pass(const DevVolume& V, const uint8_t* _
   const RayTrim t = ray_trim(V, r);
   df total{0.f, 0.f};
   bool fl = false;
+  float lo, hi;
+  cutoff_bounds(cut, r.dX.h, r.dY.h, r.dZ.h, lo, hi);
   walk_segments(w, occ, [&](int i, float& ia, float& c) {
     ia = t.ia[i];
     c = t.c[i];
   }, s, [&](int kb, int js, int je) {
-    const float p = march_block<STORE, EXACT>(V, r, kb, js, je, cut);
+    const float p = march_block<STORE, EXACT>(V, r, kb, js, je, lo, hi, cut);
     if (!EXACT && block_flagged(p))
       fl = true;
     else

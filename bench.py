@@ -138,7 +138,7 @@ def device_sms():
     return torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
 
 
-def roofline(phase, samples, pixels, marched, slots, sm_mhz):
+def roofline(phase, samples, pixels, marched, slots, sm_mhz, nexact=0):
     """The dominant kernel (k_ray) against the limit it is bound by.
 
     k_ray marches FP32 samples whose taps come from L1/L2 (every volume is
@@ -146,7 +146,8 @@ def roofline(phase, samples, pixels, marched, slots, sm_mhz):
     `frac` is the issue fraction: warp instructions per launch (ncu,
     profiles/k_ray_counters_batch_300.json, scaled to this launch by marched
     samples) over SMs x 4 schedulers x the sampled SM clock x the launch's
-    CUDA-event time.  Beside it: the marched gather bytes (16 B per marched
+    CUDA-event time (the ray phase holds k_ray_fix too, whose instructions,
+    scaled by the rays it marches, are added).  Beside it: the marched gather bytes (16 B per marched
     sample + 4 B per DRR pixel) against the L2 read bandwidth measured here
     (frac_l2), the DRAM traffic against the HBM copy peak (frac_hbm), and the
     algorithmic bytes of the reference's march (16 B per sample of the whole
@@ -167,6 +168,9 @@ def roofline(phase, samples, pixels, marched, slots, sm_mhz):
     kr = profile_counts("k_ray")
     if kr and kr.get("marched_per_launch"):
         inst = kr["inst_per_launch"] * marched / kr["marched_per_launch"]
+        kf = profile_counts("k_ray_fix")
+        if kf and kf.get("exact_cutoff_rays_per_launch"):
+            inst += kf["inst_per_launch"] * nexact / kf["exact_cutoff_rays_per_launch"]
         out.update(achieved=inst / ray_s / 1e9, peak=issue_peak / 1e9, frac=inst / ray_s / issue_peak,
                    inst_per_launch=inst)
         traffic = kr["dram_bytes_per_launch"] * marched / kr["marched_per_launch"]
@@ -378,7 +382,7 @@ def main():
     marched, slots = cnt[2], cnt[3]
     nexact = C.c_int()
     L.call("asc_engine_exact_rays", eng.handle, C.byref(nexact))
-    rl = roofline(phase, samples.value, pixels.value, marched, slots, clk.summary().get("sm_mhz"))
+    rl = roofline(phase, samples.value, pixels.value, marched, slots, clk.summary().get("sm_mhz"), nexact.value)
     # ---- plain per-pose drop-in form on the same GPU (sampled)
     plain_v = None
     if not args.no_plain:
