@@ -456,8 +456,8 @@ def run_tracking(args):
     L.call("asc_device_sync")
     t0 = time.perf_counter()
     # Tracker::optimize frame after frame, each from the previous frame's pose
-    poses, cost, evals = eng.track(images, start, method=0, n_particles=64, n_iter=30, lo=-3.0, hi=3.0, seed=100,
-                                   guess=1, repeats=1)
+    poses, cost, evals = eng.track(images, start, method=0, n_particles=64, n_iter=30, lo=-3.0, hi=3.0,
+                                   seed=args.seed, guess=1, repeats=1)
     dt = time.perf_counter() - t0
     e = np.abs(poses - np.stack([traj[b] for b in range(2)], 1))  # frames x bones x 6
     fm, fd = e[:, :, :3].max(axis=(1, 2)), e[:, :, 3:].max(axis=(1, 2))  # per frame, worst bone and axis
@@ -487,6 +487,7 @@ def run_tracking(args):
             "lost_bone_frames": len(lost),
             "lost_where_cost_prefers_tracked_pose": prefers_tracked,
             "lost_worst_axis_counts_xyzypr": worst_axes.astype(int).tolist(),
+            "first_lost_frame": int(min(f for f, _ in lost)) if lost else None, "seed": args.seed,
             "data": "synthetic sinusoidal trajectory, 250 fps"}
 
 
@@ -706,6 +707,7 @@ if __name__ == "__main__":
         ap.add_argument("--max-frames", type=int, default=5, help="serving: frames per job drawn from 1..max")
         ap.add_argument("--pso-iters", type=int, default=10, help="serving: PSO iterations per frame")
         ap.add_argument("--max-jobs", type=int, default=8, help="serving: jobs admitted at once")
+        ap.add_argument("--seed", type=int, default=100, help="tracking: the swarms' random seed")
         ap.add_argument("--particles", type=int, default=100, help="roofline: candidates per bone")
         ap.add_argument("--reps", type=int, default=3, help="roofline: evaluations")
         ap.add_argument("--storage", default="u16", choices=["u16", "f16", "bf16", "f32"],
