@@ -2,10 +2,11 @@
 // for many (bone, manipulator) candidates per pass, with the scene resident
 // on the device.
 //
-// One evaluation is five launches on one stream (six with cf_model 1):
+// One evaluation is six launches on one stream (seven with cf_model 1):
 //   k_setup_iv    a thread per (item, view): FP64 pose composition, view
 //                            matrix, viewport (Tracker.cpp:603-634) and crop;
 //   k_setup       1 block:  the tile layout of every crop, with prefix sums;
+//   k_tile_map    grid-stride: each ray and view tile's (item, view);
 //   k_ray         persistent: 16x16-ray tiles pulled from an atomic queue,
 //                            DRRs written to a packed buffer; rays with a
 //                            sample within rounding of the cutoff are listed;
@@ -105,6 +106,7 @@ struct IV {
   int view, slot;  // the engine view and the bone's slot of this (item, view)
   int rtx, rty, ftx, fty;
   int err;        // the crop exceeded the render size (the reference throws)
+  float band[3];  // the bone's cutoff here: raw - t0, hi0 + t0, t1 (k_ray's band)
   long long pix;  // offset of this crop in the DRR buffer
 };
 
@@ -133,6 +135,8 @@ struct Bufs {
   unsigned* ivt;   // per-iv tile tickets
   unsigned* itt;   // per-item view tickets
   int* fixt;       // ray tiles holding rays to march again exactly (k_ray_fix)
+  int* rtile_iv;   // per ray tile: its (item, view) (k_tile_map)
+  int* ftile_iv;   // per view tile: its (item, view)
   Counters* C;
 };
 
@@ -193,6 +197,10 @@ __device__ void setup_iv(const SceneDev* __restrict__ sc, int k, const int* __re
   frame_inverse(mv, imv);
   frame_row_matrix(imv, imv16);
   fold_matrix(imv16, B.inv_scale, B.inv_trans, r.m);
+  const Cutoff& cut = B.cut[j];
+  r.band[0] = cut.raw - cut.t0;
+  r.band[1] = cut.hi0 + cut.t0;
+  r.band[2] = cut.t1;
   double vc = 0.0;
   if (!calculate_viewport(mv, V.cam, V.ip, B.inv_scale, B.inv_trans, vp)) {
     vc = 9999.0;  // Tracker.cpp:614-617
@@ -314,6 +322,20 @@ __global__ void __launch_bounds__(1024) k_setup(const SceneDev* __restrict__ sc,
   }
 }
 
+// Every ray tile's and view tile's (item, view), so that the persistent
+// kernels look a grabbed tile up with one load instead of a binary search
+// over the prefix sums (ten dependent loads while the block waits).
+// (Dealing most ray tiles to the blocks in turn, with a queue for the rest,
+// measured 9 % slower: a block then owns fixed columns of every crop, and the
+// central ones cost more.)
+__global__ void __launch_bounds__(256) k_tile_map(Bufs b)
+{
+  const int rt = b.C->rtiles, ft = b.C->ftiles, n = b.C->n_iv;
+  const int stride = gridDim.x * blockDim.x;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < rt; t += stride) b.rtile_iv[t] = find_iv(b.roff, n, t);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ft; t += stride) b.ftile_iv[t] = find_iv(b.foff, n, t);
+}
+
 // ---------------------------------------------------------------- k_ray
 #ifndef ASC_RAY_MINBLOCKS
 #define ASC_RAY_MINBLOCKS 4  // 4 x 256 threads resident per SM (<= 64 registers)
@@ -393,10 +415,9 @@ __global__ void __launch_bounds__(NRAY, ASC_RAY_MINBLOCKS) k_ray(const SceneDev*
       s_tile = tl;
       int kk = 0;
       if (tl < b.C->rtiles) {
-        kk = find_iv(b.roff, b.C->n_iv, tl);
-        const IV& q = b.iv[kk];
-        const Cutoff& c = sc->bones[q.bone].cut[q.slot];
-        s_band = make_float4(c.raw - c.t0, c.hi0 + c.t0, c.t1, 0.f);
+        kk = b.rtile_iv[tl];
+        const float* bd = b.iv[kk].band;
+        s_band = make_float4(bd[0], bd[1], bd[2], 0.f);
       }
       s_k = kk;
     }
@@ -537,7 +558,7 @@ __global__ void __launch_bounds__(FIX_THREADS) k_ray_fix(const SceneDev* __restr
   const int nw = gridDim.x * (FIX_THREADS / 32);
   for (int w = blockIdx.x * (FIX_THREADS / 32) + wib; w < nt; w += nw) {
     const int tile = b.fixt[w];
-    const int k = find_iv(b.roff, b.C->n_iv, tile);
+    const int k = b.rtile_iv[tile];
     const IV& r = b.iv[k];
     const int t = tile - b.roff[k];
     const int x0 = (t % r.rtx) * RTX, y0 = (t / r.rtx) * RTY;
@@ -890,7 +911,7 @@ __global__ void __launch_bounds__(VNT, ASC_VIEW_MINBLOCKS)
     if (threadIdx.x == 0) {
       const int tl = atomicAdd(&b.C->fnext, 1);
       s_tile = tl;
-      s_k = tl < b.C->ftiles ? find_iv(b.foff, b.C->n_iv, tl) : 0;
+      s_k = tl < b.C->ftiles ? b.ftile_iv[tl] : 0;
     }
     __syncthreads();
     const int tile = s_tile, k = s_k;
@@ -1087,7 +1108,7 @@ __global__ void __launch_bounds__(256) k_sad(const SceneDev* __restrict__ sc, Bu
   __shared__ bool s_last;
   const int nv = sc->slots, ftiles = b.C->ftiles;
   for (int tile = blockIdx.x; tile < ftiles; tile += gridDim.x) {
-    const int k = find_iv(b.foff, b.C->n_iv, tile);
+    const int k = b.ftile_iv[tile];
     const IV& r = b.iv[k];
     const int t = tile - b.foff[k];
     const int tx0 = (t % r.ftx) * VT, ty0 = (t / r.ftx) * VT;
@@ -1490,6 +1511,7 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
   if (!err) err = e->alloc(e->b.foff, n_iv + 1);
   if (!err) err = e->alloc(e->b.drr, n_iv * (size_t)rw * rh);
   if (!err) err = e->alloc(e->b.part, n_iv * tiles);
+  if (!err) err = e->alloc(e->b.ftile_iv, n_iv * tiles);
   if (!err && cf_model) err = e->alloc(e->b.fg, n_iv * (size_t)rw * rh);
   if (!err && cf_model) err = e->alloc(e->b.hmean, n_iv);
   if (!err && cf_model) err = e->alloc(e->b.tsad, n_iv * tiles);
@@ -1498,6 +1520,7 @@ ASC_API int asc_engine_create(int n_views, const asc_view_desc* views, int n_bon
   if (!err) err = e->alloc(e->b.itt, (size_t)max_items);
   // at most every ray tile of a full batch
   if (!err) err = e->alloc(e->b.fixt, n_iv * (size_t)((rw + RTX - 1) / RTX) * ((rh + RTY - 1) / RTY));
+  if (!err) err = e->alloc(e->b.rtile_iv, n_iv * (size_t)((rw + RTX - 1) / RTX) * ((rh + RTY - 1) / RTY));
   if (!err) err = e->alloc(e->b.C, 1);
   if (!err) err = e->alloc(e->d_bone, (size_t)max_items);
   if (!err) err = e->alloc(e->d_manip, (size_t)max_items * 6);
@@ -1772,6 +1795,7 @@ static int engine_launch(asc_engine e, int n, const int* bone, const double* man
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[0], s));
   k_setup_iv<<<(n * e->host.slots + 127) / 128, 128, 0, s>>>(e->dev, n, bone, manip, e->b);
   k_setup<<<1, 1024, 0, s>>>(e->dev, n, e->b, cost);
+  k_tile_map<<<e->sms * 2, 256, 0, s>>>(e->b);
   if (prof) ASC_CUDA(cudaEventRecord(e->ev[1], s));
   k_ray<<<e->sms * e->launch.ray_blocks_per_sm, NRAY, 0, s>>>(e->dev, e->b, g_empty_skip, e->launch.ray_shape);
   k_ray_fix<<<e->sms * 4, FIX_THREADS, 0, s>>>(e->dev, e->b, g_empty_skip);

@@ -404,9 +404,9 @@ def main():
                 "vs_baseline": None, "dtype": "f32 (u16 volumes, FP64 pose/NCC combine)", "data": "synthetic",
                 "config": dict(CONFIG, l2="256 MB memset between timed steps", parallelism=f"replicas x{ws}"),
                 "e2e": {"value": e2e, "unit": "pose-evals/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-                # per step: k_pso_init, then per iteration one graph of seven kernels
-                # (k_pso_update, k_setup_iv, k_setup, k_ray, k_ray_fix, k_view, k_pso_best)
-                "gpu_launches": args.steps * (1 + 7 * iters),
+                # per step: k_pso_init, then per iteration one graph of eight kernels (k_pso_update,
+                # k_setup_iv, k_setup, k_tile_map, k_ray, k_ray_fix, k_view, k_pso_best)
+                "gpu_launches": args.steps * (1 + 8 * iters),
                 "roofline": rl,
                 "kernel_ms": {"setup": phase[0], "ray": phase[1], "view": phase[2]},
                 "launch": launch,
