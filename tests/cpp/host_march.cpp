@@ -103,3 +103,42 @@ extern "C" void hm_occupancy(const uint16_t* vol, int nx, int ny, int nz, float 
         ++counts[b];
       }
 }
+
+// Soundness of the cutoff band (Cutoff): every sample of every ray of the
+// image, its FP32 value as the march computes it (a one-sample march block
+// with the band below every value, so the block returns the value itself)
+// and the exact decision (sample_above).  counts[0] = samples, [1] = samples
+// whose FP32 decision (v > raw) differs from the exact one, [2] = such
+// samples outside the ray's band, [3] = samples in the band.
+extern "C" void hm_band(const uint16_t* vol, int nx, int ny, int nz, const float* m, const float* vp, float step,
+                        float cutoff, int w, int h, long long* counts)
+{
+  std::vector<uint32_t> pairs(padded_words(nx, ny, nz, ASC_STORE_U16));
+  pack_pairs(nx, ny, nz, ASC_STORE_U16, [&](int x, int y, int z) { return (uint32_t)vol[((size_t)z * ny + y) * nx + x]; },
+             pairs.data());
+  const int px = nx + 2 * PAD, pxy = px * (ny + 2 * PAD);
+  DevVolume V{pairs.data(), nx, ny, nz, px, pxy, ASC_STORE_U16, 1.0f / 65535.0f, 0.f};
+  V.gmax = volume_gmax(nx, ny, nz, [&](int x, int y, int z) { return (float)vol[((size_t)z * ny + y) * nx + x]; });
+  const Cutoff cut = make_cutoff(cutoff, V.norm, V.gmax);
+  counts[0] = counts[1] = counts[2] = counts[3] = 0;
+  df sx, sy;
+  df_split((double)vp[2] / (double)w, sx.h, sx.l);
+  df_split((double)vp[3] / (double)h, sy.h, sy.l);
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) {
+      RaySetup r;
+      if (!ray_setup(m, vp, x, y, sx, sy, step, nx, ny, nz, r)) continue;
+      float lo, hi;
+      cutoff_bounds(cut, r.dX.h, r.dY.h, r.dZ.h, lo, hi);
+      for (int k = 0; k < r.K; ++k) {
+        const int kb = k - k % REBASE, j = k % REBASE;
+        const float v = march_block<ASC_STORE_U16, false>(V, r, kb, j, j, -INFINITY, -INFINITY, cut);
+        const bool fp32 = v > cut.raw, exact = sample_above<ASC_STORE_U16>(V, r, k, cut);
+        const bool in_band = v > lo && v < hi;
+        ++counts[0];
+        counts[1] += fp32 != exact;
+        counts[2] += fp32 != exact && !in_band;
+        counts[3] += in_band;
+      }
+    }
+}

@@ -24,6 +24,8 @@ def hm(tmp_path_factory):
     lib.hm_raycast.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
     lib.hm_occupancy.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_void_p]
+    lib.hm_band.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_float,
+                            C.c_int, C.c_int, C.c_void_p]
     return lib
 
 
@@ -157,3 +159,40 @@ def test_cutoff_at_a_voxel_level_decides_as_fp64(hm):
                             float(np.float32(rp.intensity)), cut, w, h)
             assert ref.max() > 0.1
             assert np.abs(got - ref).max() < 1e-6
+
+
+@pytest.mark.parametrize("level,noise", [(200, 0.0), (200, 20.0)])
+def test_cutoff_band_holds_every_fp32_misdecision(hm, level, noise):
+    """The march decides a sample in FP32 only outside its ray's band
+    (Cutoff: the bound on the FP32 value's error).  For every sample of every
+    ray, with the cutoff at a voxel level (c = float32(level / 65535), where
+    FP32 and exact decisions part), on a noise-free phantom (a plateau at the
+    cutoff) and a noisy one: each sample whose FP32 decision (v > raw)
+    differs from the exact one lies inside the band."""
+    shape = (40, 36, 44)
+    sc = S.make_scene([shape], 1.0, (96, 96), 1.0, filters="sobel", seed=4)
+    sc.volumes[0].data = S.phantom(shape, seed=4, noise=noise)
+    if noise == 0.0:
+        assert (sc.volumes[0].data == level).any()
+    tr = O.Tracker(sc)
+    cut = float(np.float32(level / 65535.0))
+    rng = np.random.default_rng(12)
+    tot = np.zeros(4, np.int64)
+    for _ in range(2):
+        pose = S.perturb(sc.truth[0], rng, 2.0, 10.0).astype(np.float64)
+        for vi in range(2):
+            ok, m, vp, w, h = tr.view_setup(0, vi, pose)
+            vd = tr.vd[0]
+            vol = np.ascontiguousarray(vd.data, np.uint16)
+            mf = np.ascontiguousarray(m, np.float32)
+            vpf = np.ascontiguousarray(vp, np.float32)
+            c = np.zeros(4, np.int64)
+            hm.hm_band(vol.ctypes.data, vd.dims[0], vd.dims[1], vd.dims[2], mf.ctypes.data, vpf.ctypes.data,
+                       float(np.float32(sc.ray[vi][0].step)), cut, w, h, c.ctypes.data)
+            tot += c
+    assert tot[0] > 10 ** 5, tot
+    assert tot[2] == 0, tot                       # every misdecision inside the band
+    if noise:
+        assert 0 < tot[3] < 1e-2 * tot[0], tot    # a narrow band that samples do meet
+    else:  # the soft tissue is a plateau at the cutoff: FP32 drops all of it, and all of it is in the band
+        assert tot[1] > 0.5 * tot[0], tot
