@@ -265,12 +265,22 @@ class Server:
     """Continuous batching of registration jobs on one SlotEngine.
 
     hbm_budget: device bytes the server may hold (engine scratch, cached
-    volumes, radiographs); max_jobs: jobs admitted at once (1 = FIFO)."""
+    volumes, radiographs); max_jobs: jobs admitted at once (1 = FIFO);
+    sat_items: a job joins running ones only while their candidates per
+    PSO iteration (particles x bones) stay below this (None: no limit).  A
+    launch of that many candidates already fills the GPU, so a job admitted
+    beyond it would only stretch the running jobs' iterations.
+    min_backlog: a job joins running ones only while at least this many jobs
+    wait (1: always).  Below the rate one GPU sustains the queue stays short
+    and jobs then run one at a time, each at full speed; under a backlog
+    they are merged."""
 
     def __init__(self, hbm_budget: float = 150e9, max_jobs: int = 8, n_views=16, n_bones=64, render=(1024, 1024),
-                 max_items=2048):
+                 max_items=2048, sat_items: Optional[int] = None, min_backlog: int = 1):
         self.budget = float(hbm_budget)
         self.max_jobs = max_jobs
+        self.sat_items = sat_items
+        self.min_backlog = min_backlog
         self.eng = SlotEngine(n_views, n_bones, render, max_items)
         self.base_bytes = engine_bytes(n_views, render[0], render[1], max_items)
         self.cache = VolumeCache()
@@ -339,6 +349,12 @@ class Server:
             while queue and len(running) < self.max_jobs and (not realtime or queue[0].arrival <= t):
                 if not self._fits(queue[0]):
                     break
+                if running and self.sat_items is not None and \
+                        sum(r["job"].particles * len(r["job"].scene.volumes) for r in running) >= self.sat_items:
+                    break
+                if running and self.min_backlog > 1 and \
+                        sum(1 for j in queue if not realtime or j.arrival <= t) < self.min_backlog:
+                    break
                 job = queue.pop(0)
                 try:
                     running.append(self._start(job, now()))
@@ -384,7 +400,8 @@ class Server:
                 "p99_latency_s": float(np.percentile(lat, 99)) if len(lat) else None,
                 "launches": launches, "mean_batch": float(np.mean(batch_items)) if batch_items else 0.0,
                 "peak_reserved_gb": self.peak / 1e9, "mean_reserved_gb": mean_occ / 1e9,
-                "cache_hits": self.cache.hits, "cache_misses": self.cache.misses, "max_jobs": self.max_jobs}
+                "cache_hits": self.cache.hits, "cache_misses": self.cache.misses, "max_jobs": self.max_jobs,
+                "sat_items": self.sat_items, "min_backlog": self.min_backlog}
 
 
 def device_memory():

@@ -519,9 +519,14 @@ def run_serving(args):
                 "jobs": int(len(lat))}
 
     res = {}
-    for name, mj in (("continuous", args.max_jobs), ("fifo", 1)):
+    modes = [("continuous", args.max_jobs, None, 1), ("fifo", 1, None, 1)]
+    if args.sat_items:
+        modes.insert(1, ("capped", args.max_jobs, args.sat_items, 1))
+    if args.min_backlog > 1:
+        modes.insert(1, ("backlog", args.max_jobs, None, args.min_backlog))
+    for name, mj, sat, mb in modes:
         js = jobs()
-        srv = serve.Server(hbm_budget=150e9, max_jobs=mj)
+        srv = serve.Server(hbm_budget=150e9, max_jobs=mj, sat_items=sat, min_backlog=mb)
         summary = srv.serve(js, realtime=True)
         summary["steady"] = steady(js)
         summary["jobs_per_s"] = len(js) / summary["wall_s"]
@@ -531,6 +536,7 @@ def run_serving(args):
     return {"workload": "serving", "metric": "sustained pose evals/s; p50/p99 job latency",
             "value": c["pose_evals_per_s"], "unit": "pose-evals/s", "rate_jobs_per_s": args.rate,
             "continuous": c, "fifo": f, "speedup_vs_fifo": c["pose_evals_per_s"] / max(f["pose_evals_per_s"], 1e-9),
+            "capped": res.get("capped"), "backlog": res.get("backlog"),
             "data": f"synthetic mixed jobs: volumes 64^3-320^3 u16, viewports 256^2-1024^2, 1-4 bones, 1-3 views, "
                     f"1-{args.max_frames} frames, PSO 32-128 particles x {args.pso_iters} iterations then simplex"}
 
@@ -708,6 +714,12 @@ if __name__ == "__main__":
         ap.add_argument("--pso-iters", type=int, default=10, help="serving: PSO iterations per frame")
         ap.add_argument("--max-jobs", type=int, default=8, help="serving: jobs admitted at once")
         ap.add_argument("--seed", type=int, default=100, help="tracking: the swarms' random seed")
+        ap.add_argument("--sat-items", type=int, default=0,
+                        help="serving: also run the merged loop that admits a job only while the running jobs' "
+                             "candidates per iteration stay below this")
+        ap.add_argument("--min-backlog", type=int, default=0,
+                        help="serving: also run the merged loop that admits a job beside running ones only while "
+                             "this many jobs wait")
         ap.add_argument("--particles", type=int, default=100, help="roofline: candidates per bone")
         ap.add_argument("--reps", type=int, default=3, help="roofline: evaluations")
         ap.add_argument("--storage", default="u16", choices=["u16", "f16", "bf16", "f32"],

@@ -62,3 +62,33 @@ def test_admission_respects_budget():
     summary = srv.serve(jobs, realtime=False)
     assert summary["failed"] == 0, [j.error for j in jobs]
     assert srv.peak <= budget
+
+
+def test_saturation_cap_admits_no_job_beside_a_full_batch():
+    """sat_items: a job joins running ones only while their candidates per
+    PSO iteration stay below the cap; with a cap below any job's own, jobs run
+    one at a time (as FIFO, in as many launches), with the same poses."""
+    fifo = _jobs()
+    n_fifo = serve.Server(hbm_budget=150e9, max_jobs=1, render=RENDER, max_items=512).serve(fifo, realtime=False)
+    capped = _jobs()
+    srv = serve.Server(hbm_budget=150e9, max_jobs=4, render=RENDER, max_items=512, sat_items=1)
+    n_cap = srv.serve(capped, realtime=False)
+    assert n_cap["failed"] == 0 and n_cap["launches"] == n_fifo["launches"], (n_cap, n_fifo)
+    for a, b in zip(fifo, capped):
+        for pa, pb in zip(a.poses, b.poses):
+            assert np.array_equal(pa, pb)
+
+
+def test_backlog_rule_runs_jobs_one_at_a_time_without_a_queue():
+    """min_backlog: with more waiting jobs required than the stream ever
+    holds, the merged loop runs the jobs one at a time (as FIFO), with the
+    same poses."""
+    fifo = _jobs()
+    n_fifo = serve.Server(hbm_budget=150e9, max_jobs=1, render=RENDER, max_items=512).serve(fifo, realtime=False)
+    held = _jobs()
+    n_held = serve.Server(hbm_budget=150e9, max_jobs=4, render=RENDER, max_items=512,
+                          min_backlog=len(held) + 1).serve(held, realtime=False)
+    assert n_held["failed"] == 0 and n_held["launches"] == n_fifo["launches"], (n_held, n_fifo)
+    for a, b in zip(fifo, held):
+        for pa, pb in zip(a.poses, b.poses):
+            assert np.array_equal(pa, pb)
