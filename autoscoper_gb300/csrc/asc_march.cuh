@@ -805,9 +805,9 @@ __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup&
   const unsigned imax = ASC_QUADS ? (unsigned)(V.nz + 2 * PAD - 1) * pxy - 1u
                                   : (unsigned)(V.nz + 2 * PAD - 1) * pxy - px - 1u;
   float acc = 0.f;
-  // > 0 once a sample fell in (lo, hi): min(v - lo, hi - v) > 0 exactly then
-  // (the sign of a rounded difference is the exact one)
-  float nearf = -1.0f;
+  // the largest sample not counted (below hi): above lo once a sample fell
+  // in the band (one max, predicated on the test that decides the add)
+  float nearf = -3.0e38f;
   // the cutoff test of sample ks with value v: adds v when above
   auto take = [&](float v, int ks) {
     if constexpr (EXACT) {
@@ -817,8 +817,10 @@ __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup&
         if (sample_above<STORE>(V, r, ks, cut)) acc += v;
       }
     } else {
-      acc += v >= hi ? v : 0.0f;
-      nearf = fmaxf(nearf, fminf(v - lo, hi - v));
+      if (v >= hi)
+        acc += v;
+      else
+        nearf = fmaxf(nearf, v);
     }
   };
   float j = (float)js;
@@ -872,7 +874,7 @@ __device__ __forceinline__ float march_block(const DevVolume& V, const RaySetup&
     take(v, kb + k);
   }
   if constexpr (EXACT) return acc;
-  return nearf > 0.0f ? -acc - 0.0f : acc;
+  return nearf > lo ? -acc - 0.0f : acc;
 }
 
 // Whether a march block's sum carries the band's mark (march_block).

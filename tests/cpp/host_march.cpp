@@ -106,8 +106,9 @@ extern "C" void hm_occupancy(const uint16_t* vol, int nx, int ny, int nz, float 
 
 // Soundness of the cutoff band (Cutoff): every sample of every ray of the
 // image, its FP32 value as the march computes it (a one-sample march block
-// with the band below every value, so the block returns the value itself)
-// and the exact decision (sample_above).  counts[0] = samples, [1] = samples
+// whose band (lo = +inf, hi = -inf) counts every value and marks none, so
+// the block returns the value itself) and the exact decision
+// (sample_above).  counts[0] = samples, [1] = samples
 // whose FP32 decision (v > raw) differs from the exact one, [2] = such
 // samples outside the ray's band, [3] = samples in the band.
 extern "C" void hm_band(const uint16_t* vol, int nx, int ny, int nz, const float* m, const float* vp, float step,
@@ -132,7 +133,7 @@ extern "C" void hm_band(const uint16_t* vol, int nx, int ny, int nz, const float
       cutoff_bounds(cut, r.dX.h, r.dY.h, r.dZ.h, lo, hi);
       for (int k = 0; k < r.K; ++k) {
         const int kb = k - k % REBASE, j = k % REBASE;
-        const float v = march_block<ASC_STORE_U16, false>(V, r, kb, j, j, -INFINITY, -INFINITY, cut);
+        const float v = march_block<ASC_STORE_U16, false>(V, r, kb, j, j, INFINITY, -INFINITY, cut);
         const bool fp32 = v > cut.raw, exact = sample_above<ASC_STORE_U16>(V, r, k, cut);
         const bool in_band = v > lo && v < hi;
         ++counts[0];
